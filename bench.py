@@ -1,0 +1,357 @@
+"""Benchmark of the GB300 EVP-FFT solver step.
+
+Workload (one GPU): 64^3 periodic-Voronoi RVE with 125 grains, Cu-like FCC
+crystal, uniaxial tension along z (lateral stresses zero), 2e-4 strain per
+increment, plain FP64.  One step = one strain increment: the prelude, the
+Green-operator fixed-point iterations until the error norms reach Err = 1e-5
+(or IterMax = 200), the increment end.  Metric: voxel-iterations per second
+= sum over steps of (voxels x Green iterations) / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl voce|reference]
+                  [--precision fp64|mixed]
+
+--impl reference times the CPU implementation of the same step (the oracle's
+C restatement of the reference, all host threads) on bounded samples.
+N > 1 (torchrun): independent replicas, one per GPU, no collective on the
+data path; the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NR_BYTES_PER_VOXEL = 528     # algorithmic bytes per voxel of one Newton kernel launch
+ITER_BYTES_PER_VOXEL = 816   # algorithmic bytes per voxel-iteration (plain FP64)
+FLUSH_BYTES = 512 << 20      # > 129 MB L2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="voce", choices=["voce", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Group:
+    """Host-side barrier and max over ranks (gloo); no GPU collective."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax = float(t[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_case():
+    from voce_gb300 import synth
+    return synth.config2(n_steps=100)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the Newton kernel from the committed ncu
+    summary (profiles/ncu_traffic.json), scaled to 64^3 by voxel count."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    k = d.get("k_nr")
+    if not k:
+        return None
+    return float(k["dram_bytes_per_launch"]) * (64 ** 3) / float(k["voxels"])
+
+
+def cpu_sample(threads: int, iters: int):
+    """The oracle (C restatement of the reference) on a bounded sample of
+    the workload: the first increment of the 64^3 case capped at `iters`
+    Green iterations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    if not os.path.exists(orc.PORT_LIB):
+        orc.build_port()
+    case = make_case()
+    case.iter_max = iters
+    d = tempfile.mkdtemp(prefix="cpu_")
+    nl = case.write(d)
+    j = orc.Job(nl, threads=threads)
+    t0 = time.perf_counter()
+    j.run(1)
+    dt = time.perf_counter() - t0
+    n_it = j.increment(0)["iters"]
+    j.close()
+    return case.mesh.nvox * n_it / dt, dt, n_it
+
+
+def run_reference(args, rank, world):
+    """--impl reference: CPU timing of the same step on all host threads."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample_iters = 10
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    if not os.path.exists(orc.PORT_LIB):
+        orc.build_port()
+    case = make_case()
+    case.iter_max = sample_iters
+    d = tempfile.mkdtemp(prefix="ref_")
+    nl = case.write(d)
+    j = orc.Job(nl, threads=threads)
+    j.run(args.warmup)
+    t0 = time.perf_counter()
+    j.run(args.steps)
+    dt = time.perf_counter() - t0
+    its = sum(j.increment(args.warmup + k)["iters"] for k in range(args.steps))
+    j.close()
+    v = case.mesh.nvox * its / dt
+    sample = ("64^3 Voronoi-125 tension, %d increments capped at %d Green iterations each "
+              "(%d iterations, %.1f s)" % (args.steps, sample_iters, its, dt))
+    out = {
+        "impl": "reference", "metric": "voxel_iterations_per_s", "value": v,
+        "unit": "voxel-iter/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "64^3 periodic Voronoi, 125 grains, Cu FCC, tension z, "
+                               "FP64, one increment per step (Green iterations capped)",
+                   "cpu_threads": threads},
+        "cpu_baseline": {"value": v, "unit": "voxel-iter/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_voce(args, rank, world, grp):
+    from voce_gb300 import capi, synth  # noqa: F401
+    lib = capi.load()
+    prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+    case = make_case()
+    nv = case.mesh.nvox
+    d = tempfile.mkdtemp(prefix="bench_")
+    nl_path = case.write(d)
+    nl = capi.read_namelist(nl_path)
+    slip = capi.read_slip(os.path.join(d, "mat.sx"))
+
+    # ---- device-resident leg: K increments timed with CUDA events --------
+    r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase, prec)
+    r.run(args.warmup)
+    r.set_profiling(True)
+    r.reset_kernel_times()
+    launches0 = r.kernel_launches
+    grp.barrier()
+    step_ms = []
+    iters = []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for k in range(args.steps):
+            r.flush_l2(FLUSH_BYTES)
+            launches0 += 1        # the flush kernel is not part of the step
+            step_ms.append(r.run_timed(1))
+            iters.append(r.increment(args.warmup + k)["iters"])
+    grp.barrier()
+    launches = r.kernel_launches - launches0
+    kt = r.kernel_times()
+    tot_ms = sum(step_ms)
+    t_max = grp.max(tot_ms)
+    vox_iters = grp.sum(float(nv * sum(iters)))
+    value = vox_iters / (t_max * 1e-3)
+    nr_ms, nr_n = kt["nr"]
+    nr_avg_s = nr_ms * 1e-3 / max(nr_n, 1)
+    peak, peak_kind = measured_peaks()
+    achieved = NR_BYTES_PER_VOXEL * nv / nr_avg_s / 1e9
+    fp64_peak = lib.voce_measure_fp64_tflops()
+    r.close()
+
+    # ---- end-to-end leg through the C ABI, host buffers ----------------
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        import numpy as np
+        eul_b = lib.voce_host_alloc(nv * 24)
+        gr_b = lib.voce_host_alloc(nv * 4)
+        ph_b = lib.voce_host_alloc(nv * 4)
+        out_b = lib.voce_host_alloc(2 * nv * 48)
+        eul = np.ctypeslib.as_array((C.c_double * (nv * 3)).from_address(eul_b)).reshape(nv, 3)
+        gr = np.ctypeslib.as_array((C.c_int * nv).from_address(gr_b))
+        ph = np.ctypeslib.as_array((C.c_int * nv).from_address(ph_b))
+        outs = np.ctypeslib.as_array((C.c_double * (2 * nv * 6)).from_address(out_b)).reshape(2, 6 * nv)
+        eul[:] = case.mesh.euler_deg
+        gr[:] = case.mesh.grain
+        ph[:] = case.mesh.phase
+        grp.barrier()
+        t0 = time.perf_counter()
+        re = capi.Rve.create(nl, slip, eul, gr, ph, prec)
+        e2e_iters = 0
+        for k in range(args.steps):
+            re.run(1)
+            e2e_iters += re.increment(k)["iters"]
+            lib.voce_rve_get_field(re._h, 20, outs[0].ctypes.data_as(C.POINTER(C.c_double)))
+            lib.voce_rve_get_field(re._h, 21, outs[1].ctypes.data_as(C.POINTER(C.c_double)))
+        re.close()
+        t_e2e = time.perf_counter() - t0
+        grp.barrier()
+        t_e2e = grp.max(t_e2e)
+        e2e = {"value": grp.sum(float(nv * e2e_iters)) / t_e2e, "unit": "voxel-iter/s",
+               "h2d_bytes_per_step": int(nv * 32 / args.steps),
+               "d2h_bytes_per_step": int(2 * 6 * 8 * nv),
+               "timed": "create from pinned host mesh + %d increments, each followed by the "
+                        "stress and strain-rate fields copied to pinned host memory" % args.steps}
+        for b in (eul_b, gr_b, ph_b, out_b):
+            lib.voce_host_free(b)
+
+    # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
+    cpu = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        v, dt, n_it = cpu_sample(threads, 40)
+        cpu = {"value": v, "unit": "voxel-iter/s", "cores": threads, "kind": "port",
+               "sample": "first increment of the same 64^3 case capped at %d Green iterations "
+                         "(%.1f s on %d threads)" % (n_it, dt, threads)}
+
+    if rank != 0:
+        return
+    out = {
+        "metric": "voxel_iterations_per_s", "value": value, "unit": "voxel-iter/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == capi.PREC_FP64 else "f64+f32fft",
+        "data": "synthetic",
+        "config": {"workload": "64^3 periodic Voronoi, 125 grains, Cu FCC (C11=168.4 GPa), "
+                               "n=20, Voce hardening, tension z 1e-3/s, 2e-4 strain per "
+                               "increment (config 2), one increment per step",
+                   "precision": args.precision, "voxels": nv,
+                   "green_iterations": iters, "l2": "flushed (512 MB write) before every step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic(),
+                     "kernel": "k_nr", "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_voxel": NR_BYTES_PER_VOXEL,
+                     "avg_launch_ms": nr_avg_s * 1e3},
+        "fp64": {"measured_peak_tflops": fp64_peak},
+        "kernel_ms": {k: v[0] for k, v in kt.items()},
+        "kernel_launches_timed": {k: v[1] for k, v in kt.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    grp = Group(world)
+    run_voce(args, rank, world, grp)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,172 @@
+/*
+ * voce_gpu.h -- C ABI of the GB300 EVP-FFT solver step (libvoce_gpu.so).
+ *
+ * Drop-in boundary for the solver step of the Voce crystal-plasticity code:
+ * the Green-operator fixed point with the per-voxel Newton-Raphson stress
+ * update and the Voce hardening law.  One RVE (representative volume
+ * element) lives whole on one GPU; every kernel on the solve path is
+ * hand-written sm_103a code in this library.  Plain C types only: no CUDA or
+ * C++ types cross this boundary.
+ *
+ * Reference interfaces each group replaces (file:line in the Voce sources):
+ *   voce_namelist_read    GetNameList           io.c:54-122 (names io.c:25-52)
+ *   voce_slip_read        PlasticInit's reader  init.c:51-186
+ *   voce_mesh_read        InitMicroStruct's reader init.c:393-442
+ *   voce_rve_create       SetupJob              init.c:617-828
+ *   voce_rve_run          Evolution (istep loop) evolution.c:265-622
+ *   voce_rve_destroy      DestroyJob            init.c:830-930
+ *   voce_rve_get_field    the field globals Sig/Eps/Edot/DisGrad/... that
+ *                         io.c's Write*MPI dump (evp.h:190-316, io.c:193-1003)
+ *   voce_rve_get_increment the vm.out line     evolution.c:562-566
+ *   voce_rve_get_iter_log  the err.out lines   evolution.c:424-429
+ *   SetupJob/Evolution/DestroyJob (voce_legacy.h) keep the reference's own
+ *                         void(void) entry points over its globals.
+ *
+ * Errors: every function returns VOCE_OK (0) or a VOCE_ERR_* code and never
+ * exits the process (the reference calls MPI_Abort or exit(35) instead:
+ * evp.h:42-43, kinematics.c:306-309).  voce_last_error() gives a message.
+ * Non-convergence (IterMax reached, Newton cap of 100 reached) is reported
+ * in the increment record, not as an error, as in the reference.
+ *
+ * Threading: one host thread per handle; handles are independent (each has
+ * its own CUDA stream).
+ */
+#ifndef VOCE_GPU_H
+#define VOCE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VOCE_ABI_VERSION 1
+
+enum {
+    VOCE_OK = 0,
+    VOCE_ERR_ARG = 1,         /* bad argument / null pointer */
+    VOCE_ERR_IO = 2,          /* file cannot be opened or read */
+    VOCE_ERR_PARSE = 3,       /* malformed input (mesh index mismatch: init.c:420-423) */
+    VOCE_ERR_BC = 4,          /* inconsistent boundary conditions (init.c:713-735) */
+    VOCE_ERR_SINGULAR = 5,    /* near-zero matrix row (kinematics.c:306-309) */
+    VOCE_ERR_UNSUPPORTED = 6, /* grid size or material this build does not handle */
+    VOCE_ERR_NOMEM = 7,       /* device allocation failed */
+    VOCE_ERR_CUDA = 8,        /* CUDA runtime error, or no GPU */
+    VOCE_ERR_STATE = 9        /* call out of order */
+};
+
+enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1 };
+
+/* Every variable the reference's namelist reader knows (io.c:25-52), with
+ * the reference's names, types and lengths. */
+typedef struct {
+    int CellDim[3];
+    int N_phases;
+    int Type_phases[2];          /* 0 crystal, 1 gas */
+    double TimeStep;
+    int N_steps;
+    int Update_Flag, Hard_Flag, Tex_Flag, IterMax;
+    int PrintControl[2];
+    double Err;
+    int VelGrad_BC_Flag[6];      /* Voigt order 11,22,33,23,13,12 */
+    double VelGrad_BC[6];
+    int Stress_BC_Flag[6];
+    double Stress_BC[6];
+    double ElastConst_PhaseI[4];  /* c11 c12 c44 nu (MPa) */
+    double ElastConst_PhaseII[4];
+    char Slip_PhaseI[100], Slip_PhaseII[100], initial_ms[100];
+    double self[2], coplane[2], cross[2], glissile[2], hirth[2], lomer[2];
+} voce_namelist;
+
+/* One slip mode of a .sx single-crystal file (init.c:117-178), as read:
+ * slip-plane normals bn and directions bb are NOT normalised here. */
+typedef struct {
+    int nsys;                    /* <= 12 */
+    double nrs, gamd0;           /* rate-sensitivity exponent, reference rate */
+    double tau0f, tau0b, tau1, thet0, thet1;  /* Voce parameters */
+    double bn[12][3], bb[12][3];
+} voce_slip;
+
+/* Microstructure: per voxel (x slowest, z fastest) Bunge angles in degrees,
+ * grain id and 1-based phase id -- the columns of the mesh file. */
+typedef struct {
+    int dims[3];
+    const double *euler_deg;     /* 3 per voxel */
+    const int *grain;
+    const int *phase;
+} voce_mesh;
+
+/* One vm.out line (evolution.c:563-564) plus the full-precision macro values
+ * behind it. */
+typedef struct {
+    int istep, iters, iter_total;
+    int nr_max;                  /* largest Newton iteration count seen */
+    double e_vm, evmp, d_vm, dvmp, s_vm, s_vm1;
+    double sig_avg[9], sig_avg1[9], eps_avg[9], edot_avg[9];
+    double disgrad_avg[9];       /* DisGradAvg_actual at increment end */
+    double err_e, err_s;         /* last iteration's normalised errors */
+    double rot_slip_avg, rot_loc_avg; /* update_orient's printed averages */
+    double nr_iters_total;       /* Newton iterations summed over voxels and iterations */
+} voce_increment;
+
+/* Field ids for voce_rve_get_field.  Tensors come back as 9 doubles per
+ * voxel (row-major 3x3) like the reference globals (evp.h:304-312). */
+enum {
+    VOCE_FIELD_SIG = 0,        /* Sig, 9 */
+    VOCE_FIELD_EPS = 1,        /* Eps, 9 */
+    VOCE_FIELD_EDOT = 2,       /* Edot (plastic strain rate), 9 */
+    VOCE_FIELD_DISGRAD = 3,    /* DisGrad, 9 */
+    VOCE_FIELD_TRANMAT = 4,    /* TranMat_xt2sa, 9 */
+    VOCE_FIELD_CRSS = 5,       /* crss (forward), 12 */
+    VOCE_FIELD_GAMDOT = 6,     /* gamdot, 12 */
+    VOCE_FIELD_GAMACUM = 7,    /* gamacum, 1 */
+    VOCE_FIELD_SVM = 8,        /* SVM, 1 */
+    VOCE_FIELD_EVM = 9,        /* EVM, 1 */
+    VOCE_FIELD_SIG_VOIGT = 20, /* Sig 11,22,33,23,13,12: the order of the
+                                  sig_1..6 dumps (io.c:321-358), 6 */
+    VOCE_FIELD_EDOT_VOIGT = 21 /* Edot in the same order (io.c:360-397), 6 */
+};
+
+typedef struct voce_rve voce_rve;
+
+int voce_abi_version(void);
+const char *voce_last_error(void);
+
+/* Input readers, same formats and quirks as the reference's. */
+int voce_namelist_read(const char *path, voce_namelist *out);
+int voce_slip_read(const char *path, voce_slip *out);
+int voce_mesh_read(const char *path, const int dims[3], double *euler_deg,
+                   int *grain, int *phase);
+
+/* Set an RVE up on the current CUDA device (SetupJob).  slip[p] is the
+ * slip mode of phase p+1 and may be NULL for a gas phase. */
+int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2],
+                    const voce_mesh *mesh, int precision, voce_rve **out);
+/* Same, reading the namelist, .sx and mesh files (relative names are taken
+ * relative to the namelist's directory). */
+int voce_rve_create_from_files(const char *namelist_path, int precision,
+                               voce_rve **out);
+/* Advance n strain increments (each: prelude, Green-operator iterations to
+ * convergence or IterMax, epilogue with reorientation and hardening). */
+int voce_rve_run(voce_rve *r, int n_increments);
+int voce_rve_increments_done(const voce_rve *r);
+int voce_rve_get_increment(const voce_rve *r, int k, voce_increment *out);
+/* Normalised errors and s_vm of every iteration of increment k (0-based);
+ * returns the number of iterations written (at most max), or < 0. */
+int voce_rve_get_iter_log(const voce_rve *r, int k, double *err_e,
+                          double *err_s, double *s_vm, int max);
+/* Full-precision record of every iteration of increment k, 12 doubles per
+ * iteration: normalised Err_e, Err_s, s_vm, Newton iterations summed over
+ * voxels, the raw sums over voxels of the strain and stress error norms (the
+ * values the reference reduces at evolution.c:406-409), and the sum over
+ * voxels of the stress 6-vector.  Returns the number of rows written. */
+int voce_rve_get_iter_detail(const voce_rve *r, int k, double *rows, int max);
+int voce_rve_get_field(voce_rve *r, int field, double *host_out);
+int voce_rve_destroy(voce_rve *r);
+
+/* Device-memory footprint of an RVE of the given grid and precision, in
+ * bytes (what voce_rve_create allocates). */
+long long voce_rve_footprint(const int dims[3], int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,54 @@
+/*
+ * voce_gpu_diag.h -- measurement and diagnostic entry points of
+ * libvoce_gpu.so.  None of these has a counterpart in the reference (it has
+ * no timers, evolution.c); they exist so that a caller can time the solver
+ * step on the RVE's own CUDA stream and attribute time to kernels.
+ */
+#ifndef VOCE_GPU_DIAG_H
+#define VOCE_GPU_DIAG_H
+
+#include "voce_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Kernel ids for voce_rve_get_kernel_time (in launch order). */
+enum {
+    VOCE_K_FFT_Z_FWD = 0,  /* r2c along z of the 6 stress components */
+    VOCE_K_FFT_Y_FWD = 1,  /* c2c along y */
+    VOCE_K_FFT_X_GREEN = 2,/* c2c along x, Green operator, inverse along x */
+    VOCE_K_FFT_Y_INV = 3,  /* c2c along y, inverse */
+    VOCE_K_FFT_Z_INV = 4,  /* c2r along z + displacement-gradient update */
+    VOCE_K_NR = 5,         /* per-voxel Newton-Raphson stress update */
+    VOCE_K_FIN_ITER = 6,   /* error norms, averages, mixed-BC update */
+    VOCE_K_PRELUDE = 7,    /* increment prelude */
+    VOCE_K_INC_FFT = 8,    /* antisymmetric update back to real space (3 launches) */
+    VOCE_K_INCR_END = 9,   /* strain update, reorientation, Voce hardening */
+    VOCE_K_FIN_INCR = 10,  /* increment averages */
+    VOCE_K_COUNT = 11
+};
+
+/* voce_rve_run bracketed by CUDA events on the RVE's stream; device_ms is
+ * the elapsed time between them. */
+int voce_rve_run_timed(voce_rve *r, int n_increments, double *device_ms);
+/* When on, every kernel launch is bracketed by an event pair; the totals
+ * accumulate until reset. */
+int voce_rve_set_profiling(voce_rve *r, int on);
+int voce_rve_get_kernel_time(const voce_rve *r, int kernel, double *ms_total,
+                             long long *timed_launches);
+int voce_rve_reset_kernel_times(voce_rve *r);
+/* Number of kernels this RVE has launched so far. */
+long long voce_rve_kernel_launches(const voce_rve *r);
+/* Write `bytes` of scratch on the RVE's stream (evicts the L2), then wait. */
+int voce_rve_flush_l2(voce_rve *r, long long bytes);
+/* Pinned host memory for inputs and results. */
+void *voce_host_alloc(long long bytes);
+void voce_host_free(void *p);
+/* FP64 FMA throughput of the current device, TFLOP/s (FMA = 2 flops). */
+double voce_measure_fp64_tflops(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

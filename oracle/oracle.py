@@ -1,0 +1,132 @@
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/_build/liboracle.so`` (the C restatement, built by
+``build_port()`` with gcc on any machine) and, where it was built from the
+reference sources, ``oracle/_ref/libevp_ref.so`` / ``oracle/_ref/evp_ref``.
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+bench.py use this module, as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
+PORT_BIN = os.path.join(HERE, "_build", "evp_oracle")
+REF_BIN = os.path.join(HERE, "_ref", "evp_ref")
+REF_LIB = os.path.join(HERE, "_ref", "libevp_ref.so")
+REFERENCE_SRC = "/root/reference"
+
+FIELDS = {"sig": (0, 9), "eps": (1, 9), "edot": (2, 9), "disgrad": (3, 9),
+          "tranmat": (4, 9), "crss": (5, 12), "gamdot": (6, 12), "gamacum": (7, 1),
+          "svm": (8, 1), "evm": (9, 1), "schmid": (10, 60), "cgr": (11, 36)}
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref() -> bool:
+    """Compile the reference sources with the shims, when they are present."""
+    if not os.path.isdir(REFERENCE_SRC):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_SRC], check=True)
+    return True
+
+
+class OracleIncr(C.Structure):
+    _fields_ = [("istep", C.c_int), ("iters", C.c_int), ("iter_total", C.c_int),
+                ("e_vm", C.c_double), ("evmp", C.c_double), ("d_vm", C.c_double),
+                ("dvmp", C.c_double), ("s_vm", C.c_double), ("s_vm1", C.c_double),
+                ("sig_avg", C.c_double * 9), ("sig_avg1", C.c_double * 9),
+                ("eps_avg", C.c_double * 9), ("edot_avg", C.c_double * 9),
+                ("disgrad_avg", C.c_double * 9), ("err_e", C.c_double),
+                ("err_s", C.c_double)]
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(PORT_LIB):
+            build_port()
+        L = C.CDLL(PORT_LIB)
+        L.oracle_create.restype = C.c_void_p
+        L.oracle_create.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_char_p]
+        L.oracle_destroy.argtypes = [C.c_void_p]
+        L.oracle_run.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_get_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_get_increment.argtypes = [C.c_void_p, C.c_int, C.POINTER(OracleIncr)]
+        L.oracle_get_iter_log.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_nvox.restype = C.c_long
+        L.oracle_nvox.argtypes = [C.c_void_p]
+        L.oracle_get_reference_medium.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_lu_inv66.argtypes = [C.c_void_p]
+        _LIB = L
+    return _LIB
+
+
+class Job:
+    """One oracle run of a namelist (reads the same files as the reference)."""
+
+    def __init__(self, namelist: str, threads: int = 1, trace: str | None = None):
+        err = C.create_string_buffer(256)
+        self._h = lib().oracle_create(namelist.encode(), threads,
+                                      trace.encode() if trace else None, err)
+        if not self._h:
+            raise RuntimeError("oracle: " + err.value.decode())
+        self.nv = lib().oracle_nvox(self._h)
+
+    def run(self, n: int) -> None:
+        lib().oracle_run(self._h, n)
+
+    def increment(self, k: int) -> dict:
+        r = OracleIncr()
+        if lib().oracle_get_increment(self._h, k, C.byref(r)) != 0:
+            raise IndexError(k)
+        return r.as_dict()
+
+    def iter_log(self, k: int):
+        n = self.increment(k)["iters"]
+        a = np.zeros((3, n))
+        lib().oracle_get_iter_log(self._h, k, a[0].ctypes.data, a[1].ctypes.data,
+                                  a[2].ctypes.data)
+        return a
+
+    def field(self, name: str) -> np.ndarray:
+        fid, w = FIELDS[name]
+        out = np.zeros((self.nv, w))
+        lib().oracle_get_field(self._h, fid, out.ctypes.data)
+        return out
+
+    def reference_medium(self):
+        c = np.zeros(36)
+        s = np.zeros(36)
+        w = C.c_double()
+        lib().oracle_get_reference_medium(self._h, c.ctypes.data, s.ctypes.data, C.byref(w))
+        return c.reshape(6, 6), s.reshape(6, 6), w.value
+
+    def close(self):
+        if self._h:
+            lib().oracle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

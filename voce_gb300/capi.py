@@ -1,0 +1,299 @@
+"""ctypes binding of libvoce_gpu.so (include/voce_gpu.h).
+
+This is the Python mirror of the library's C ABI: the same entry points,
+argument meanings and status codes.  It loads the in-tree library built by
+``voce_gb300.build`` and fails loudly when it is missing -- there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libvoce_gpu.so")
+
+VOCE_OK = 0
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
+          5: "ERR_SINGULAR", 6: "ERR_UNSUPPORTED", 7: "ERR_NOMEM", 8: "ERR_CUDA",
+          9: "ERR_STATE"}
+PREC_FP64, PREC_MIXED = 0, 1
+FIELD = {"sig": 0, "eps": 1, "edot": 2, "disgrad": 3, "tranmat": 4, "crss": 5,
+         "gamdot": 6, "gamacum": 7, "svm": 8, "evm": 9, "sig_voigt": 20,
+         "edot_voigt": 21}
+FIELD_WIDTH = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 12, 7: 1, 8: 1, 9: 1,
+               20: 6, 21: 6}
+
+
+class VoceNamelist(C.Structure):
+    _fields_ = [
+        ("CellDim", C.c_int * 3), ("N_phases", C.c_int), ("Type_phases", C.c_int * 2),
+        ("TimeStep", C.c_double), ("N_steps", C.c_int),
+        ("Update_Flag", C.c_int), ("Hard_Flag", C.c_int), ("Tex_Flag", C.c_int),
+        ("IterMax", C.c_int), ("PrintControl", C.c_int * 2), ("Err", C.c_double),
+        ("VelGrad_BC_Flag", C.c_int * 6), ("VelGrad_BC", C.c_double * 6),
+        ("Stress_BC_Flag", C.c_int * 6), ("Stress_BC", C.c_double * 6),
+        ("ElastConst_PhaseI", C.c_double * 4), ("ElastConst_PhaseII", C.c_double * 4),
+        ("Slip_PhaseI", C.c_char * 100), ("Slip_PhaseII", C.c_char * 100),
+        ("initial_ms", C.c_char * 100),
+        ("self", C.c_double * 2), ("coplane", C.c_double * 2), ("cross", C.c_double * 2),
+        ("glissile", C.c_double * 2), ("hirth", C.c_double * 2), ("lomer", C.c_double * 2),
+    ]
+
+
+class VoceSlip(C.Structure):
+    _fields_ = [
+        ("nsys", C.c_int), ("nrs", C.c_double), ("gamd0", C.c_double),
+        ("tau0f", C.c_double), ("tau0b", C.c_double), ("tau1", C.c_double),
+        ("thet0", C.c_double), ("thet1", C.c_double),
+        ("bn", (C.c_double * 3) * 12), ("bb", (C.c_double * 3) * 12),
+    ]
+
+
+class VoceMesh(C.Structure):
+    _fields_ = [("dims", C.c_int * 3), ("euler_deg", C.POINTER(C.c_double)),
+                ("grain", C.POINTER(C.c_int)), ("phase", C.POINTER(C.c_int))]
+
+
+class VoceIncrement(C.Structure):
+    _fields_ = [
+        ("istep", C.c_int), ("iters", C.c_int), ("iter_total", C.c_int), ("nr_max", C.c_int),
+        ("e_vm", C.c_double), ("evmp", C.c_double), ("d_vm", C.c_double), ("dvmp", C.c_double),
+        ("s_vm", C.c_double), ("s_vm1", C.c_double),
+        ("sig_avg", C.c_double * 9), ("sig_avg1", C.c_double * 9),
+        ("eps_avg", C.c_double * 9), ("edot_avg", C.c_double * 9),
+        ("disgrad_avg", C.c_double * 9), ("err_e", C.c_double), ("err_s", C.c_double),
+        ("rot_slip_avg", C.c_double), ("rot_loc_avg", C.c_double),
+        ("nr_iters_total", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+# every function declared in include/voce_gpu.h: (name, restype, argtypes)
+PROTOTYPES = [
+    ("voce_abi_version", C.c_int, []),
+    ("voce_last_error", C.c_char_p, []),
+    ("voce_namelist_read", C.c_int, [C.c_char_p, C.POINTER(VoceNamelist)]),
+    ("voce_slip_read", C.c_int, [C.c_char_p, C.POINTER(VoceSlip)]),
+    ("voce_mesh_read", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("voce_rve_create", C.c_int, [C.POINTER(VoceNamelist), C.POINTER(C.POINTER(VoceSlip)),
+                                  C.POINTER(VoceMesh), C.c_int, C.POINTER(C.c_void_p)]),
+    ("voce_rve_create_from_files", C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    ("voce_rve_run", C.c_int, [C.c_void_p, C.c_int]),
+    ("voce_rve_increments_done", C.c_int, [C.c_void_p]),
+    ("voce_rve_get_increment", C.c_int, [C.c_void_p, C.c_int, C.POINTER(VoceIncrement)]),
+    ("voce_rve_get_iter_log", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
+    ("voce_rve_get_iter_detail", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
+    ("voce_rve_get_field", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_rve_destroy", C.c_int, [C.c_void_p]),
+    ("voce_rve_footprint", C.c_longlong, [C.POINTER(C.c_int), C.c_int]),
+    # voce_gpu_diag.h
+    ("voce_rve_run_timed", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_rve_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
+    ("voce_rve_get_kernel_time", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_longlong)]),
+    ("voce_rve_reset_kernel_times", C.c_int, [C.c_void_p]),
+    ("voce_rve_kernel_launches", C.c_longlong, [C.c_void_p]),
+    ("voce_rve_flush_l2", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("voce_host_alloc", C.c_void_p, [C.c_longlong]),
+    ("voce_host_free", None, [C.c_void_p]),
+    ("voce_measure_fp64_tflops", C.c_double, []),
+]
+KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
+           "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
+
+_LIB: Optional[C.CDLL] = None
+
+
+class VoceError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libvoce_gpu.so.  Raises if the library has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError("libvoce_gpu.so is not built (%s); run "
+                           "`python -m voce_gb300.build`" % path)
+    lib = C.CDLL(path)
+    for name, res, args in PROTOTYPES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != VOCE_OK:
+        raise VoceError(rc, load().voce_last_error().decode(errors="replace"))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def read_namelist(path: str) -> VoceNamelist:
+    nl = VoceNamelist()
+    _check(load().voce_namelist_read(path.encode(), C.byref(nl)))
+    return nl
+
+
+def read_slip(path: str) -> VoceSlip:
+    s = VoceSlip()
+    _check(load().voce_slip_read(path.encode(), C.byref(s)))
+    return s
+
+
+def read_mesh(path: str, dims: Sequence[int]):
+    nv = int(np.prod(dims))
+    eul = np.zeros((nv, 3))
+    grain = np.zeros(nv, dtype=np.int32)
+    phase = np.zeros(nv, dtype=np.int32)
+    d = (C.c_int * 3)(*dims)
+    _check(load().voce_mesh_read(path.encode(), d, _dptr(eul), _iptr(grain), _iptr(phase)))
+    return eul, grain, phase
+
+
+def footprint(dims: Sequence[int], precision: int = PREC_FP64) -> int:
+    return int(load().voce_rve_footprint((C.c_int * 3)(*dims), precision))
+
+
+class Rve:
+    """One RVE resident on the GPU (the handle of include/voce_gpu.h)."""
+
+    def __init__(self, handle: C.c_void_p, dims):
+        self._h = handle
+        self.dims = tuple(dims)
+        self.nv = int(np.prod(self.dims))
+
+    @classmethod
+    def from_files(cls, namelist_path: str, precision: int = PREC_FP64) -> "Rve":
+        lib = load()
+        h = C.c_void_p()
+        _check(lib.voce_rve_create_from_files(namelist_path.encode(), precision, C.byref(h)))
+        nl = read_namelist(namelist_path)
+        return cls(h, tuple(nl.CellDim))
+
+    @classmethod
+    def create(cls, nl: VoceNamelist, slip: VoceSlip, euler_deg: np.ndarray,
+               grain: np.ndarray, phase: np.ndarray, precision: int = PREC_FP64,
+               solid_phase: int = 0) -> "Rve":
+        lib = load()
+        eul = np.ascontiguousarray(euler_deg, dtype=np.float64)
+        gr = np.ascontiguousarray(grain, dtype=np.int32)
+        ph = np.ascontiguousarray(phase, dtype=np.int32)
+        mesh = VoceMesh()
+        mesh.dims = (C.c_int * 3)(*nl.CellDim)
+        mesh.euler_deg = _dptr(eul)
+        mesh.grain = _iptr(gr)
+        mesh.phase = _iptr(ph)
+        sp = (C.POINTER(VoceSlip) * 2)()
+        sp[solid_phase] = C.pointer(slip)
+        h = C.c_void_p()
+        _check(lib.voce_rve_create(C.byref(nl), sp, C.byref(mesh), precision, C.byref(h)))
+        return cls(h, tuple(nl.CellDim))
+
+    def run(self, n: int) -> None:
+        _check(load().voce_rve_run(self._h, n))
+
+    @property
+    def increments_done(self) -> int:
+        return load().voce_rve_increments_done(self._h)
+
+    def increment(self, k: int) -> dict:
+        r = VoceIncrement()
+        _check(load().voce_rve_get_increment(self._h, k, C.byref(r)))
+        return r.as_dict()
+
+    def iter_log(self, k: int, max_iters: int = 100000):
+        ee = np.zeros(max_iters)
+        es = np.zeros(max_iters)
+        sv = np.zeros(max_iters)
+        n = load().voce_rve_get_iter_log(self._h, k, _dptr(ee), _dptr(es), _dptr(sv), max_iters)
+        if n < 0:
+            _check(-n)
+        return ee[:n], es[:n], sv[:n]
+
+    def run_timed(self, n: int) -> float:
+        """Run n increments; returns device milliseconds between CUDA events
+        recorded on the RVE's stream before and after."""
+        ms = C.c_double()
+        _check(load().voce_rve_run_timed(self._h, n, C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on: bool) -> None:
+        _check(load().voce_rve_set_profiling(self._h, int(on)))
+
+    def kernel_times(self) -> dict:
+        out = {}
+        for k, name in enumerate(KERNELS):
+            ms = C.c_double()
+            n = C.c_longlong()
+            _check(load().voce_rve_get_kernel_time(self._h, k, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def reset_kernel_times(self) -> None:
+        _check(load().voce_rve_reset_kernel_times(self._h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(load().voce_rve_kernel_launches(self._h))
+
+    def flush_l2(self, nbytes: int = 512 << 20) -> None:
+        _check(load().voce_rve_flush_l2(self._h, nbytes))
+
+    def iter_detail(self, k: int, max_iters: int = 100000) -> np.ndarray:
+        """Rows of 12 per iteration: err_e, err_s, s_vm, newton_sum,
+        sum_conv_e, sum_conv_s, sum of the stress 6-vector (6)."""
+        rows = np.zeros((max_iters, 12))
+        n = load().voce_rve_get_iter_detail(self._h, k, _dptr(rows), max_iters)
+        if n < 0:
+            _check(-n)
+        return rows[:n]
+
+    def field(self, name: str) -> np.ndarray:
+        fid = FIELD[name]
+        w = FIELD_WIDTH[fid]
+        out = np.zeros(self.nv * w)
+        _check(load().voce_rve_get_field(self._h, fid, _dptr(out)))
+        if fid in (20, 21):
+            return out.reshape(w, self.nv)
+        return out.reshape(self.nv, w)
+
+    def close(self) -> None:
+        if self._h:
+            load().voce_rve_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,868 @@
+// Host side of libvoce_gpu.so: input readers, material setup, RVE lifecycle
+// and the C ABI declared in include/voce_gpu.h.
+#include "voce_gpu.h"
+#include "voce_gpu_diag.h"
+#include "voce_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace voce;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                        \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? VOCE_ERR_NOMEM : VOCE_ERR_CUDA,  \
+                        "%s: %s", #x, cudaGetErrorString(e_));                             \
+    } while (0)
+
+// ---- Lebensohn-Tome basis (kinematics.c:346-364) on the host ------------
+double HB[6][3][3];
+bool hb_ready = false;
+
+void hb_init()
+{
+    if (hb_ready) return;
+    std::memset(HB, 0, sizeof(HB));
+    HB[1][0][0] = -1. * RSQ6; HB[1][1][1] = -1. * RSQ6; HB[1][2][2] = 2. * RSQ6;
+    HB[0][0][0] = -1. * RSQ2; HB[0][1][1] = RSQ2;
+    HB[2][1][2] = RSQ2; HB[2][2][1] = RSQ2;
+    HB[3][0][2] = RSQ2; HB[3][2][0] = RSQ2;
+    HB[4][0][1] = RSQ2; HB[4][1][0] = RSQ2;
+    HB[5][0][0] = RSQ3; HB[5][1][1] = RSQ3; HB[5][2][2] = RSQ3;
+    hb_ready = true;
+}
+
+// chg_basis opt 2 (3x3 -> nb-vector) and opt 4 (3x3x3x3 -> 6x6), opt 3
+void t_to_v(const double t[3][3], double *v, int nb)
+{
+    for (int i = 0; i < nb; ++i) {
+        double s = 0.0;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) s += t[a][b] * HB[i][a][b];
+        v[i] = s;
+    }
+}
+
+void t4_to_c66(const double *t4, double *c)
+{
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double s = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    for (int k = 0; k < 3; ++k)
+                        for (int l = 0; l < 3; ++l)
+                            s += t4[((a * 3 + b) * 3 + k) * 3 + l] * HB[i][a][b] * HB[j][k][l];
+            c[i * 6 + j] = s;
+        }
+}
+
+void c66_to_t4(const double *c, double *t4)
+{
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    double s = 0.0;
+                    for (int i = 0; i < 6; ++i)
+                        for (int j = 0; j < 6; ++j) s += c[i * 6 + j] * HB[i][a][b] * HB[j][k][l];
+                    t4[((a * 3 + b) * 3 + k) * 3 + l] = s;
+                }
+}
+
+// LU_inv_66: Crout LU with implicit scaling and the reference's TINY pivot
+// rule (kinematics.c:282-424).  Returns false on a near-zero row.
+bool lu_inv66(double c[6][6])
+{
+    const int n = 6;
+    double vv[6], y[6][6];
+    int indx[6], imax = 0;
+    for (int i = 0; i < n; ++i) {
+        double big = 0.0, t;
+        for (int j = 0; j < n; ++j)
+            if ((t = std::fabs(c[i][j])) > big) big = t;
+        if (std::fabs(big) < 1E-5) return false;
+        vv[i] = 1.0 / big;
+    }
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < j; ++i) {
+            double s = c[i][j];
+            for (int k = 0; k < i; ++k) s -= c[i][k] * c[k][j];
+            c[i][j] = s;
+        }
+        double big = 0.0, dum;
+        for (int i = j; i < n; ++i) {
+            double s = c[i][j];
+            for (int k = 0; k < j; ++k) s -= c[i][k] * c[k][j];
+            c[i][j] = s;
+            if ((dum = vv[i] * std::fabs(s)) >= big) { big = dum; imax = i; }
+        }
+        if (j != imax) {
+            for (int k = 0; k < n; ++k) std::swap(c[imax][k], c[j][k]);
+            vv[imax] = vv[j];
+        }
+        indx[j] = imax;
+        if (std::fabs(c[j][j]) < 1E-5) c[j][j] = 1.0E-20;
+        if (j != n - 1) {
+            dum = 1.0 / c[j][j];
+            for (int i = j + 1; i < n; ++i) c[i][j] *= dum;
+        }
+    }
+    for (int jc = 0; jc < n; ++jc) {
+        double b[6] = {0, 0, 0, 0, 0, 0};
+        b[jc] = 1.0;
+        int ii = -1;
+        for (int i = 0; i < n; ++i) {
+            int ip = indx[i];
+            double s = b[ip];
+            b[ip] = b[i];
+            if (ii >= 0)
+                for (int q = ii; q < i; ++q) s -= c[i][q] * b[q];
+            else if (std::fabs(s) > 1E-5) ii = i;
+            b[i] = s;
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double s = b[i];
+            for (int q = i + 1; q < n; ++q) s -= c[i][q] * b[q];
+            b[i] = s / c[i][i];
+        }
+        for (int i = 0; i < n; ++i) y[i][jc] = b[i];
+    }
+    std::memcpy(c, y, sizeof(y));
+    return true;
+}
+
+bool fft_plan(int L, FftPlan1 &p)
+{
+    p.L = L;
+    p.nst = 0;
+    int m = L;
+    while (m % 4 == 0 && p.nst < VOCE_MAXRAD) { p.rad[p.nst++] = 4; m /= 4; }
+    while (m % 2 == 0 && p.nst < VOCE_MAXRAD) { p.rad[p.nst++] = 2; m /= 2; }
+    while (m % 3 == 0 && p.nst < VOCE_MAXRAD) { p.rad[p.nst++] = 3; m /= 3; }
+    return m == 1 && L >= 2;
+}
+
+}  // namespace
+
+// ===========================================================================
+// the RVE object
+// ===========================================================================
+struct voce_rve {
+    int precision = 0;
+    RveDesc d{};
+    SetupConst sc{};
+    Tiles tiles{};
+    int npart = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> dev_allocs;
+    int *h_flag = nullptr;  // pinned
+    double *d_out = nullptr;
+    double *d_flush = nullptr;
+    long long flush_n = 0;
+    Prof prof;
+    int n_done = 0, n_steps = 0;
+    std::vector<voce_increment> incr;
+    std::vector<std::vector<double>> itlog;
+    ~voce_rve()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        for (void *p : dev_allocs) cudaFree(p);
+        if (d_out) cudaFree(d_out);
+        if (d_flush) cudaFree(d_flush);
+        if (h_flag) cudaFreeHost(h_flag);
+        for (int k = 0; k < 2 * K_COUNT; ++k)
+            if (prof.ev[k]) cudaEventDestroy(prof.ev[k]);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+template <typename T>
+int dalloc(voce_rve *r, T *&p, size_t count)
+{
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+    if (e != cudaSuccess)
+        return fail(VOCE_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    r->dev_allocs.push_back(q);
+    p = (T *)q;
+    return VOCE_OK;
+}
+
+template <typename C, typename R>
+std::vector<C> twiddles(int L)
+{
+    std::vector<C> t(L);
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int j = 0; j < L; ++j) {
+        long double a = two_pi * (long double)j / (long double)L;
+        t[j].x = (R)cosl(a);
+        t[j].y = (R)(-sinl(a));
+    }
+    return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int voce_abi_version(void) { return VOCE_ABI_VERSION; }
+const char *voce_last_error(void) { return g_err.c_str(); }
+
+// ---------------------------------------------------------------------------
+// readers
+// ---------------------------------------------------------------------------
+
+// GetNameList (io.c:54-122): 80-byte lines, '#' and empty lines skipped, a
+// line with no first token ends the read, case-sensitive keys, unknown keys
+// ignored (so the shipped input's "Hirth" never sets hirth), a repeated key
+// keeps its first values, missing values leave the variable unchanged.
+int voce_namelist_read(const char *path, voce_namelist *nl)
+{
+    if (!path || !nl) return fail(VOCE_ERR_ARG, "null argument");
+    std::memset(nl, 0, sizeof(*nl));
+    struct Var { const char *name; int type; int len; void *ptr; };
+    Var vars[] = {
+        {"CellDim", 0, 3, nl->CellDim}, {"N_phases", 0, 1, &nl->N_phases},
+        {"Type_phases", 0, 2, nl->Type_phases}, {"TimeStep", 1, 1, &nl->TimeStep},
+        {"N_steps", 0, 1, &nl->N_steps}, {"Update_Flag", 0, 1, &nl->Update_Flag},
+        {"Hard_Flag", 0, 1, &nl->Hard_Flag}, {"Tex_Flag", 0, 1, &nl->Tex_Flag},
+        {"IterMax", 0, 1, &nl->IterMax}, {"PrintControl", 0, 2, nl->PrintControl},
+        {"Err", 1, 1, &nl->Err}, {"VelGrad_BC_Flag", 0, 6, nl->VelGrad_BC_Flag},
+        {"VelGrad_BC", 1, 6, nl->VelGrad_BC}, {"Stress_BC_Flag", 0, 6, nl->Stress_BC_Flag},
+        {"Stress_BC", 1, 6, nl->Stress_BC}, {"ElastConst_PhaseI", 1, 4, nl->ElastConst_PhaseI},
+        {"ElastConst_PhaseII", 1, 4, nl->ElastConst_PhaseII}, {"Slip_PhaseI", 2, 1, nl->Slip_PhaseI},
+        {"Slip_PhaseII", 2, 1, nl->Slip_PhaseII}, {"initial_ms", 2, 1, nl->initial_ms},
+        {"self", 1, 2, nl->self}, {"coplane", 1, 2, nl->coplane}, {"cross", 1, 2, nl->cross},
+        {"glissile", 1, 2, nl->glissile}, {"hirth", 1, 2, nl->hirth}, {"lomer", 1, 2, nl->lomer},
+    };
+    const int nvars = (int)(sizeof(vars) / sizeof(vars[0]));
+    bool seen[32] = {false};
+    FILE *fp = std::fopen(path, "r");
+    if (!fp) return fail(VOCE_ERR_IO, "cannot open namelist '%s'", path);
+    char buf[80];
+    while (true) {
+        if (!std::fgets(buf, 80, fp)) break;
+        if (std::feof(fp)) break;
+        if (buf[0] == '#' || buf[0] == '\n') continue;
+        char *save = nullptr;
+        char *tok = strtok_r(buf, " \t\n", &save);
+        if (!tok) break;
+        for (int k = 0; k < nvars; ++k) {
+            if (std::strcmp(tok, vars[k].name) != 0) continue;
+            if (!seen[k]) {
+                seen[k] = true;
+                for (int q = 0; q < vars[k].len; ++q) {
+                    tok = strtok_r(nullptr, ", \t\n", &save);
+                    if (!tok) continue;
+                    if (vars[k].type == 0) ((int *)vars[k].ptr)[q] = (int)std::atol(tok);
+                    else if (vars[k].type == 1) ((double *)vars[k].ptr)[q] = std::atof(tok);
+                    else std::snprintf((char *)vars[k].ptr, 100, "%s", tok);
+                }
+            }
+            break;
+        }
+    }
+    std::fclose(fp);
+    return VOCE_OK;
+}
+
+// PlasticInit's reader (init.c:65-186): fixed line positions, one mode used
+int voce_slip_read(const char *path, voce_slip *out)
+{
+    if (!path || !out) return fail(VOCE_ERR_ARG, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    FILE *fp = std::fopen(path, "r");
+    if (!fp) return fail(VOCE_ERR_IO, "cannot open .sx '%s'", path);
+    char buf[80] = {0};
+    auto L = [&]() { if (!std::fgets(buf, 80, fp)) buf[0] = 0; };
+    int nmax = 0, nmodes = 0, imode[16] = {0};
+    L(); L(); L(); L(); L(); L(); L(); L(); std::sscanf(buf, "%d", &nmax);
+    L(); L(); L(); std::sscanf(buf, "%d", &nmodes);
+    if (nmodes < 1 || nmodes > 16) { std::fclose(fp); return fail(VOCE_ERR_PARSE, "%s: bad N_modes", path); }
+    L(); L();
+    for (int i = 0; i < nmodes; ++i) { L(); std::sscanf(buf, "%d", &imode[i]); }
+    L();
+    int found = 0, mx = 0;
+    for (int i = 0; i < nmax; ++i) {
+        L();
+        std::sscanf(buf, "%*s %*s %d %*s", &mx);
+        bool match = false;
+        for (int q = 0; q < nmodes; ++q) if (mx == imode[q]) match = true;
+        if (!match) { for (int q = 0; q < 24; ++q) L(); continue; }
+        ++found;
+        double twsh, hs, hl;
+        int isect;
+        L(); L(); std::sscanf(buf, "%d %lf %lf %lf %d", &out->nsys, &out->nrs, &out->gamd0, &twsh, &isect);
+        if (out->nsys < 1 || out->nsys > VOCE_NS) { std::fclose(fp); return fail(VOCE_ERR_UNSUPPORTED, "nsmx %d", out->nsys); }
+        L(); L(); std::sscanf(buf, "%lf %lf %lf %lf %lf", &out->tau0f, &out->tau0b, &out->tau1, &out->thet0, &out->thet1);
+        L(); L(); std::sscanf(buf, "%lf %lf", &hs, &hl);
+        L();
+        for (int s = 0; s < out->nsys; ++s) {
+            L();
+            std::sscanf(buf, "%lf %lf %lf %lf %lf %lf", &out->bn[s][0], &out->bn[s][1], &out->bn[s][2],
+                        &out->bb[s][0], &out->bb[s][1], &out->bb[s][2]);
+        }
+    }
+    std::fclose(fp);
+    if (!found) return fail(VOCE_ERR_PARSE, "%s: selected mode not found", path);
+    return VOCE_OK;
+}
+
+// InitMicroStruct's reader (init.c:410-433): one line per voxel
+// "phi1 Phi phi2 i j k grain phase", x slowest / z fastest, 1-based.
+int voce_mesh_read(const char *path, const int dims[3], double *eul, int *grain, int *phase)
+{
+    if (!path || !dims || !eul || !grain || !phase) return fail(VOCE_ERR_ARG, "null argument");
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return fail(VOCE_ERR_IO, "cannot open mesh '%s'", path);
+    std::fseek(fp, 0, SEEK_END);
+    long sz = std::ftell(fp);
+    std::fseek(fp, 0, SEEK_SET);
+    std::vector<char> txt((size_t)sz + 1);
+    size_t got = std::fread(txt.data(), 1, (size_t)sz, fp);
+    std::fclose(fp);
+    txt[got] = 0;
+    const long long nv = (long long)dims[0] * dims[1] * dims[2];
+    char *p = txt.data();
+    for (long long v = 0; v < nv; ++v) {
+        char *e;
+        double a[3];
+        long iv[5];
+        for (int q = 0; q < 3; ++q) {
+            a[q] = std::strtod(p, &e);
+            if (e == p) return fail(VOCE_ERR_PARSE, "mesh '%s': short line at voxel %lld", path, v);
+            p = e;
+        }
+        for (int q = 0; q < 5; ++q) {
+            iv[q] = std::strtol(p, &e, 10);
+            if (e == p) return fail(VOCE_ERR_PARSE, "mesh '%s': short line at voxel %lld", path, v);
+            p = e;
+        }
+        while (*p && *p != '\n') ++p;
+        if (*p) ++p;
+        long long idx = ((iv[0] - 1) * (long long)dims[1] + iv[1] - 1) * dims[2] + iv[2] - 1;
+        if (idx != v)
+            return fail(VOCE_ERR_PARSE, "mesh '%s': inconsistent index system at voxel %lld", path, v);
+        eul[3 * v] = a[0]; eul[3 * v + 1] = a[1]; eul[3 * v + 2] = a[2];
+        grain[v] = (int)iv[3];
+        phase[v] = (int)iv[4];
+    }
+    return VOCE_OK;
+}
+
+long long voce_rve_footprint(const int dims[3], int precision)
+{
+    const long long nv = (long long)dims[0] * dims[1] * dims[2];
+    const long long nspec = (long long)(dims[2] / 2 + 1) * dims[0] * dims[1];
+    const long long cplx = precision == VOCE_PREC_MIXED ? 8 : 16;
+    // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
+    // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
+    // svm 1, evm 1, rotl 3  (= 211) + phase (4 bytes)
+    return nv * (211 * 8 + 4) + nspec * 9 * cplx;
+}
+
+// ---------------------------------------------------------------------------
+// SetupJob (init.c:617-828)
+// ---------------------------------------------------------------------------
+int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voce_mesh *mesh,
+                    int precision, voce_rve **out)
+{
+    if (!nl || !mesh || !out || !mesh->euler_deg || !mesh->phase) return fail(VOCE_ERR_ARG, "null argument");
+    *out = nullptr;
+    hb_init();
+    const int nx = nl->CellDim[0], ny = nl->CellDim[1], nz = nl->CellDim[2];
+    if (mesh->dims[0] != nx || mesh->dims[1] != ny || mesh->dims[2] != nz)
+        return fail(VOCE_ERR_ARG, "mesh dims differ from CellDim");
+    FftPlan1 plx, ply, plz;
+    if (!fft_plan(nx, plx) || !fft_plan(ny, ply) || !fft_plan(nz, plz) || nz % 2)
+        return fail(VOCE_ERR_UNSUPPORTED, "grid %dx%dx%d: each edge must be 2^a 3^b >= 2 and nz even", nx, ny, nz);
+    if (nl->N_phases < 1 || nl->N_phases > 2) return fail(VOCE_ERR_UNSUPPORTED, "N_phases %d", nl->N_phases);
+    int solid_phase = -1;
+    for (int p = 0; p < nl->N_phases; ++p)
+        if (!nl->Type_phases[p]) {
+            if (solid_phase >= 0) return fail(VOCE_ERR_UNSUPPORTED, "more than one crystalline phase");
+            solid_phase = p;
+        }
+    if (solid_phase < 0 || !slip || !slip[solid_phase]) return fail(VOCE_ERR_ARG, "no slip data for the crystal phase");
+    const voce_slip &sx = *slip[solid_phase];
+    if (sx.nsys < 1 || sx.nsys > VOCE_NS) return fail(VOCE_ERR_UNSUPPORTED, "nsys %d", sx.nsys);
+    // boundary conditions (init.c:713-745)
+    if (nl->VelGrad_BC_Flag[0] + nl->VelGrad_BC_Flag[1] + nl->VelGrad_BC_Flag[2] == 2)
+        return fail(VOCE_ERR_BC, "Cannot enforce only two deviatoric components (VelGrad_BC_Flag)");
+    for (int i = 0; i < 6; ++i)
+        if ((nl->Stress_BC_Flag[i] * nl->VelGrad_BC_Flag[i] != 0) ||
+            ((nl->Stress_BC_Flag[i] + nl->VelGrad_BC_Flag[i]) != 1))
+            return fail(VOCE_ERR_BC, "Check boundary conditions on strain rate and stress");
+    const long long nv = (long long)nx * ny * nz;
+    for (long long v = 0; v < nv; ++v)
+        if (mesh->phase[v] < 1 || mesh->phase[v] > nl->N_phases)
+            return fail(VOCE_ERR_PARSE, "phase id %d at voxel %lld", mesh->phase[v], v);
+
+    voce_rve *r = new voce_rve();
+    r->precision = precision == VOCE_PREC_MIXED ? 1 : 0;
+    RveDesc &d = r->d;
+    SetupConst &sc = r->sc;
+    d.nx = nx; d.ny = ny; d.nz = nz; d.nzh = nz / 2 + 1;
+    d.nv = nv;
+    d.nspec = (long long)d.nzh * nx * ny;
+    d.plx = plx; d.ply = ply; d.plz = plz;
+    d.mixed = r->precision;
+    for (int p = 0; p < 2; ++p) d.solid[p + 1] = (p < nl->N_phases && !nl->Type_phases[p]) ? 1 : 0;
+    d.nsys = sx.nsys;
+    d.update_flag = nl->Update_Flag;
+    d.hard_flag = nl->Hard_Flag;
+    d.iter_max = nl->IterMax;
+    d.err_tol = nl->Err;
+    d.dt = nl->TimeStep;
+    const int Nxyz = nx * ny * nz;
+    d.wgt = 1. / Nxyz;
+    d.inv_nv = 1.0 / (double)Nxyz;
+    r->n_steps = nl->N_steps;
+
+    // material (ElastStiffnessMatrix init.c:9-49, PlasticInit init.c:51-391)
+    const double *ec = solid_phase == 0 ? nl->ElastConst_PhaseI : nl->ElastConst_PhaseII;
+    double C4[81] = {0};
+    for (int i = 0; i < 3; ++i) C4[((i * 3 + i) * 3 + i) * 3 + i] = ec[0];
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k)
+            if (i != k) {
+                C4[((i * 3 + i) * 3 + k) * 3 + k] = ec[1];
+                C4[((i * 3 + k) * 3 + i) * 3 + k] = ec[2];
+                C4[((i * 3 + k) * 3 + k) * 3 + i] = ec[2];
+            }
+    t4_to_c66(C4, sc.cxt);
+    {
+        double s[6][6];
+        std::memcpy(s, sc.cxt, sizeof(s));
+        if (!lu_inv66(s)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular crystal stiffness"); }
+        std::memcpy(sc.sxt, s, sizeof(s));
+    }
+    double tau1 = sx.tau1, thet0 = sx.thet0;
+    if (tau1 < 1.E-6) { tau1 = 1.E-6; thet0 = sx.thet1; }  // init.c:141-144
+    double nr = sx.nrs;
+    d.ipow_n = (nr >= 1.0 && nr <= 256.0 && std::floor(nr) == nr) ? (int)nr : -1;
+    for (int s = 0; s < sx.nsys; ++s) {
+        d.gam0[s] = sx.gamd0;
+        d.nrs[s] = nr;
+        d.g0n[s] = sx.gamd0 * nr;
+        d.tau0[s] = sx.tau0f;
+        sc.tau0b[s] = sx.tau0b;
+        d.tau1[s] = tau1;
+        d.thet0[s] = thet0;
+        d.thet1[s] = sx.thet1;
+        double n[3], b[3];
+        double nn = std::sqrt(std::pow(sx.bn[s][0], 2.0) + std::pow(sx.bn[s][1], 2.0) + std::pow(sx.bn[s][2], 2.0));
+        double nb = std::sqrt(std::pow(sx.bb[s][0], 2.0) + std::pow(sx.bb[s][1], 2.0) + std::pow(sx.bb[s][2], 2.0));
+        for (int q = 0; q < 3; ++q) { n[q] = sx.bn[s][q] / nn; b[q] = sx.bb[s][q] / nb; }
+        double dot = n[0] * b[0] + n[1] * b[1] + n[2] * b[2];
+        if (dot > 1E-3) { delete r; return fail(VOCE_ERR_PARSE, "slip system %d is not orthogonal", s + 1); }
+        double a[3][3];
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) a[p][q] = (n[p] * b[q] + n[q] * b[p]) / 2.0;
+        t_to_v(a, sc.schxt + 5 * s, 5);
+        for (int q = 0; q < 3; ++q) { d.bn[3 * s + q] = n[q]; d.bb[3 * s + q] = b[q]; }
+    }
+    {
+        // latent hardening pattern of the 12 {111}<110> systems (init.c:283-381)
+        static const char tbl[12][13] = {
+            "SCCHGLXGGHLG", " SCGXGGHLLHG", "  SLGHGLHGGX", "   SCCHLGXGG",
+            "    SCLHGGHL", "     SGGXGLH", "      SCCHGL", "       SCGXG",
+            "        SLGH", "         SCC", "          SC", "           S"};
+        const int ph = solid_phase;
+        for (int p = 0; p < 12; ++p)
+            for (int q = p; q < 12; ++q) {
+                double v = 0.0;
+                switch (tbl[p][q]) {
+                case 'S': v = nl->self[ph]; break;
+                case 'C': v = nl->coplane[ph]; break;
+                case 'X': v = nl->cross[ph]; break;
+                case 'G': v = nl->glissile[ph]; break;
+                case 'H': v = nl->hirth[ph]; break;
+                case 'L': v = nl->lomer[ph]; break;
+                }
+                d.hard[p * VOCE_NS + q] = v;
+                d.hard[q * VOCE_NS + p] = v;
+            }
+    }
+    // boundary conditions: Udot, Scauchy, creep (init.c:716-745)
+    const double *vb = nl->VelGrad_BC, *sb = nl->Stress_BC;
+    const double U[9] = {vb[0], vb[5], vb[4], vb[5], vb[1], vb[3], vb[4], vb[3], vb[2]};
+    const double S[9] = {sb[0], sb[5], sb[4], sb[5], sb[1], sb[3], sb[4], sb[3], sb[2]};
+    std::memcpy(d.Udot, U, sizeof(U));
+    std::memcpy(d.Scauchy, S, sizeof(S));
+    int creep = 0;
+    for (int i = 0; i < 6; ++i) creep += nl->Stress_BC_Flag[i];
+    d.creep = creep / 6;
+    for (int i = 0; i < 6; ++i) { d.vflag[i] = nl->VelGrad_BC_Flag[i]; d.sflag[i] = nl->Stress_BC_Flag[i]; }
+    {
+        double us[6] = {U[0], U[4], U[8], 0.5 * (U[5] + U[7]), 0.5 * (U[2] + U[6]), 0.5 * (U[1] + U[3])};
+        t6_to_b<double>(us, d.u6);
+        d.ua[0] = 0.5 * (U[5] - U[7]);
+        d.ua[1] = 0.5 * (U[2] - U[6]);
+        d.ua[2] = 0.5 * (U[1] - U[3]);
+        double ud[6];
+        for (int q = 0; q < 6; ++q) ud[q] = us[q] * d.dt;
+        t6_to_b<double>(ud, sc.d6);
+        double s6[6] = {S[0], S[4], S[8], S[5], S[2], S[1]};
+        t6_to_b<double>(s6, sc.sc6);
+    }
+
+    // device memory
+    CUDA_TRY(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    const long long sm_count = 152;
+    long long nb = (nv + 127) / 128;
+    r->npart = (int)(nb < sm_count * 8 ? nb : sm_count * 8);
+    d.npart = r->npart;
+    int rc = VOCE_OK;
+#define AL(ptr, n) if ((rc = dalloc(r, ptr, (size_t)(n))) != VOCE_OK) { delete r; return rc; }
+    AL(d.sig, 6 * nv); AL(d.sigp, 6 * nv); AL(d.eps, 5 * nv); AL(d.dgs, 6 * nv); AL(d.dga, 3 * nv);
+    AL(d.tm, 9 * nv); AL(d.sch, 60 * nv); AL(d.sg, 21 * nv); AL(d.crss, 24 * nv); AL(d.itau, 24 * nv);
+    AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
+    AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.phase, nv);
+    AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
+    AL(d.macro, 1);
+    AL(d.itlog, (size_t)VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
+    d.incr_cap = 1;
+    AL(d.incr, 1);
+    const size_t csz = r->precision ? sizeof(float2) : sizeof(double2);
+    {
+        char *p;
+        AL(p, 6 * d.nspec * csz); d.spec = p;
+        AL(p, 3 * d.nspec * csz); d.aacc = p;
+        const int Ls[3] = {nx, ny, nz};
+        const void **tws[3] = {&d.twx, &d.twy, &d.twz};
+        for (int a = 0; a < 3; ++a) {
+            AL(p, (size_t)Ls[a] * csz);
+            if (r->precision) {
+                auto t = twiddles<float2, float>(Ls[a]);
+                CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
+            } else {
+                auto t = twiddles<double2, double>(Ls[a]);
+                CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(double2), cudaMemcpyHostToDevice));
+            }
+            *tws[a] = p;
+        }
+    }
+    double *d_eul = nullptr;
+    AL(d_eul, 3 * nv);
+#undef AL
+    CUDA_TRY(cudaMemcpyAsync(d_eul, mesh->euler_deg, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(d.phase, mesh->phase, sizeof(int) * nv, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMallocHost(&r->h_flag, 64));
+    long long nph1 = 0;
+    for (long long v = 0; v < nv; ++v) nph1 += mesh->phase[v] == 1;
+    d.wgt_ph1 = (1.0 * (double)nph1) / Nxyz;
+
+    CUDA_TRY(launch_setup(d, sc, d_eul, r->npart, r->stream));
+    std::vector<double> part((size_t)3 * r->npart * VOCE_NPART);
+    CUDA_TRY(cudaMemcpyAsync(part.data(), d.part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    // C066 = WGT * sum over voxels of C_gr (init.c:450-456), block partials
+    // summed in block order
+    double sums[48] = {0};
+    for (int pass = 0; pass < 3; ++pass)
+        for (int b = 0; b < r->npart; ++b)
+            for (int q = 0; q < VOCE_NPART - 1; ++q)
+                sums[pass * (VOCE_NPART - 1) + q] += part[((size_t)pass * r->npart + b) * VOCE_NPART + q];
+    double C066[6][6], S066[6][6];
+    for (int q = 0; q < 36; ++q) C066[q / 6][q % 6] = sums[1 + q] * d.wgt;
+    std::memcpy(S066, C066, sizeof(S066));
+    if (!lu_inv66(S066)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066"); }
+    std::memcpy(d.S0, S066, sizeof(S066));
+    double C0t[81];
+    c66_to_t4(&C066[0][0], C0t);
+    c66_to_t4(&S066[0][0], d.S0t);
+    // acoustic-tensor coefficients: K_ik = sum_jl C0_ijkl n_j n_l
+    {
+        const int P[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
+        for (int a = 0; a < 6; ++a)
+            for (int m = 0; m < 6; ++m) {
+                const int i = P[a][0], k = P[a][1], j = P[m][0], l = P[m][1];
+                double v = C0t[((i * 3 + j) * 3 + k) * 3 + l];
+                if (j != l) v += C0t[((i * 3 + l) * 3 + k) * 3 + j];
+                d.Kq[a * 6 + m] = v;
+            }
+    }
+    // macro state (InitFields init.c:494-499, 536; Evolution locals)
+    MacroDev m;
+    std::memset(&m, 0, sizeof(m));
+    for (int q = 0; q < 9; ++q) m.DisGradAvg[q] = U[q] * d.dt;
+    {
+        double dev[3][3], dvm = 0.0, us6[6];
+        double Us[3][3] = {{U[0], U[1], U[2]}, {U[3], U[4], U[5]}, {U[6], U[7], U[8]}};
+        t_to_v(Us, us6, 6);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                double s = 0.0;
+                for (int i = 0; i < 5; ++i) s += us6[i] * HB[i][a][b];
+                dev[a][b] = s;
+            }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) dvm += std::pow(dev[a][b], 2.0);
+        m.d_vm = std::sqrt(2. / 3. * dvm);
+        m.e_vm = m.d_vm * d.dt;
+    }
+    m.istep = 1;
+    m.first_iter = 1;
+    m.Err_e = 2. * d.err_tol;
+    m.Err_s = 2. * d.err_tol;
+    CUDA_TRY(cudaMemcpyAsync(d.macro, &m, sizeof(m), cudaMemcpyHostToDevice, r->stream));
+    if (r->precision) r->tiles.choose<float>(d);
+    else r->tiles.choose<double>(d);
+    CUDA_TRY(set_smem_limits(r->precision != 0, r->tiles, d));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    *out = r;
+    return VOCE_OK;
+}
+
+int voce_rve_create_from_files(const char *namelist_path, int precision, voce_rve **out)
+{
+    if (!namelist_path || !out) return fail(VOCE_ERR_ARG, "null argument");
+    voce_namelist nl;
+    int rc = voce_namelist_read(namelist_path, &nl);
+    if (rc) return rc;
+    std::string dir;
+    const char *sl = std::strrchr(namelist_path, '/');
+    if (sl) dir.assign(namelist_path, sl - namelist_path + 1);
+    auto rel = [&](const char *f) { return (f[0] == '/') ? std::string(f) : dir + f; };
+    voce_slip sx[2];
+    const voce_slip *sp[2] = {nullptr, nullptr};
+    for (int p = 0; p < nl.N_phases && p < 2; ++p) {
+        if (nl.Type_phases[p]) continue;
+        rc = voce_slip_read(rel(p == 0 ? nl.Slip_PhaseI : nl.Slip_PhaseII).c_str(), &sx[p]);
+        if (rc) return rc;
+        sp[p] = &sx[p];
+    }
+    const long long nv = (long long)nl.CellDim[0] * nl.CellDim[1] * nl.CellDim[2];
+    if (nv <= 0) return fail(VOCE_ERR_PARSE, "CellDim missing");
+    std::vector<double> eul(3 * nv);
+    std::vector<int> grain(nv), phase(nv);
+    rc = voce_mesh_read(rel(nl.initial_ms).c_str(), nl.CellDim, eul.data(), grain.data(), phase.data());
+    if (rc) return rc;
+    voce_mesh mesh;
+    std::memcpy(mesh.dims, nl.CellDim, sizeof(mesh.dims));
+    mesh.euler_deg = eul.data();
+    mesh.grain = grain.data();
+    mesh.phase = phase.data();
+    return voce_rve_create(&nl, sp, &mesh, precision, out);
+}
+
+// ---------------------------------------------------------------------------
+// Evolution (evolution.c:265-622), n increments at a time
+// ---------------------------------------------------------------------------
+int voce_rve_run(voce_rve *r, int n)
+{
+    if (!r || n < 0) return fail(VOCE_ERR_ARG, "bad argument");
+    RveDesc &d = r->d;
+    for (int k = 0; k < n; ++k) {
+        CUDA_TRY(launch_prelude(d, r->stream, r->prof));
+        int guard = 0;
+        while (true) {
+            cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, r->prof)
+                                         : launch_iteration<double>(d, r->tiles, r->npart, r->stream, r->prof);
+            if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "iteration launch: %s", cudaGetErrorString(e));
+            CUDA_TRY(cudaMemcpyAsync(r->h_flag, &d.macro->converged, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
+            CUDA_TRY(cudaStreamSynchronize(r->stream));
+            r->prof.collect();
+            if (*r->h_flag) break;
+            if (++guard > d.iter_max + 1) return fail(VOCE_ERR_STATE, "iteration control lost");
+        }
+        // copy the iteration log before the increment end resets the counters
+        MacroDev m;
+        CUDA_TRY(cudaMemcpyAsync(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost, r->stream));
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        std::vector<double> log((size_t)VOCE_ITLOG * m.iter);
+        if (m.iter)
+            CUDA_TRY(cudaMemcpyAsync(log.data(), d.itlog, sizeof(double) * log.size(), cudaMemcpyDeviceToHost, r->stream));
+        cudaError_t e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, r->prof)
+                                     : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, r->prof);
+        if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "increment-end launch: %s", cudaGetErrorString(e));
+        IncrDev rec;
+        CUDA_TRY(cudaMemcpyAsync(&rec, d.incr, sizeof(rec), cudaMemcpyDeviceToHost, r->stream));
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        r->prof.collect();
+        // one record slot, reused every increment (incr_cap == 1)
+        voce_increment o;
+        std::memset(&o, 0, sizeof(o));
+        o.istep = rec.istep; o.iters = rec.iters; o.iter_total = rec.iter_total; o.nr_max = rec.nr_max;
+        o.e_vm = rec.e_vm; o.evmp = rec.evmp; o.d_vm = rec.d_vm; o.dvmp = rec.dvmp;
+        o.s_vm = rec.s_vm; o.s_vm1 = rec.s_vm1;
+        std::memcpy(o.sig_avg, rec.sig_avg, sizeof(o.sig_avg));
+        std::memcpy(o.sig_avg1, rec.sig_avg1, sizeof(o.sig_avg1));
+        std::memcpy(o.eps_avg, rec.eps_avg, sizeof(o.eps_avg));
+        std::memcpy(o.edot_avg, rec.edot_avg, sizeof(o.edot_avg));
+        std::memcpy(o.disgrad_avg, rec.disgrad_avg, sizeof(o.disgrad_avg));
+        o.err_e = rec.err_e; o.err_s = rec.err_s;
+        o.rot_slip_avg = rec.rsl; o.rot_loc_avg = rec.rlc;
+        o.nr_iters_total = rec.nr_total;
+        r->incr.push_back(o);
+        r->itlog.push_back(std::move(log));
+        r->n_done++;
+    }
+    return VOCE_OK;
+}
+
+int voce_rve_increments_done(const voce_rve *r) { return r ? r->n_done : -1; }
+
+int voce_rve_get_increment(const voce_rve *r, int k, voce_increment *out)
+{
+    if (!r || !out || k < 0 || k >= (int)r->incr.size()) return fail(VOCE_ERR_ARG, "bad increment index");
+    *out = r->incr[k];
+    return VOCE_OK;
+}
+
+int voce_rve_get_iter_log(const voce_rve *r, int k, double *ee, double *es, double *sv, int max)
+{
+    if (!r || k < 0 || k >= (int)r->itlog.size()) return -fail(VOCE_ERR_ARG, "bad increment index");
+    const std::vector<double> &l = r->itlog[k];
+    int n = (int)(l.size() / VOCE_ITLOG);
+    if (n > max) n = max;
+    for (int i = 0; i < n; ++i) {
+        if (ee) ee[i] = l[VOCE_ITLOG * i];
+        if (es) es[i] = l[VOCE_ITLOG * i + 1];
+        if (sv) sv[i] = l[VOCE_ITLOG * i + 2];
+    }
+    return n;
+}
+
+int voce_rve_get_iter_detail(const voce_rve *r, int k, double *rows, int max)
+{
+    if (!r || k < 0 || k >= (int)r->itlog.size()) return -fail(VOCE_ERR_ARG, "bad increment index");
+    const std::vector<double> &l = r->itlog[k];
+    int n = (int)(l.size() / VOCE_ITLOG);
+    if (n > max) n = max;
+    if (rows) std::memcpy(rows, l.data(), sizeof(double) * VOCE_ITLOG * (size_t)n);
+    return n;
+}
+
+int voce_rve_get_field(voce_rve *r, int field, double *host_out)
+{
+    if (!r || !host_out) return fail(VOCE_ERR_ARG, "null argument");
+    int per;
+    switch (field) {
+    case 0: case 1: case 2: case 3: case 4: per = 9; break;
+    case 5: case 6: per = 12; break;
+    case 7: case 8: case 9: per = 1; break;
+    case 20: case 21: per = 6; break;
+    default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
+    }
+    if (!r->d_out) CUDA_TRY(cudaMalloc(&r->d_out, sizeof(double) * 12 * r->d.nv));
+    CUDA_TRY(launch_field_out(r->d, field, r->d_out, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(host_out, r->d_out, sizeof(double) * per * r->d.nv, cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return VOCE_OK;
+}
+
+int voce_rve_destroy(voce_rve *r)
+{
+    delete r;
+    return VOCE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// measurement and diagnostics (voce_gpu_diag.h)
+// ---------------------------------------------------------------------------
+int voce_rve_run_timed(voce_rve *r, int n, double *device_ms)
+{
+    if (!r || !device_ms) return fail(VOCE_ERR_ARG, "null argument");
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, r->stream));
+    int rc = voce_rve_run(r, n);
+    if (rc == VOCE_OK) {
+        CUDA_TRY(cudaEventRecord(e1, r->stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        *device_ms = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int voce_rve_set_profiling(voce_rve *r, int on)
+{
+    if (!r) return fail(VOCE_ERR_ARG, "null argument");
+    if (on && !r->prof.ev[0])
+        for (int k = 0; k < 2 * K_COUNT; ++k) CUDA_TRY(cudaEventCreate(&r->prof.ev[k]));
+    r->prof.on = on != 0;
+    return VOCE_OK;
+}
+
+int voce_rve_get_kernel_time(const voce_rve *r, int kernel, double *ms_total, long long *timed_launches)
+{
+    if (!r || kernel < 0 || kernel >= K_COUNT) return fail(VOCE_ERR_ARG, "bad kernel id");
+    if (ms_total) *ms_total = r->prof.ms[kernel];
+    if (timed_launches) *timed_launches = r->prof.n[kernel];
+    return VOCE_OK;
+}
+
+int voce_rve_reset_kernel_times(voce_rve *r)
+{
+    if (!r) return fail(VOCE_ERR_ARG, "null argument");
+    for (int k = 0; k < K_COUNT; ++k) { r->prof.ms[k] = 0.0; r->prof.n[k] = 0; }
+    return VOCE_OK;
+}
+
+long long voce_rve_kernel_launches(const voce_rve *r) { return r ? r->prof.launches : -1; }
+
+int voce_rve_flush_l2(voce_rve *r, long long bytes)
+{
+    if (!r || bytes <= 0) return fail(VOCE_ERR_ARG, "bad argument");
+    long long n = bytes / 8;
+    if (n > r->flush_n) {
+        if (r->d_flush) cudaFree(r->d_flush);
+        r->d_flush = nullptr;
+        CUDA_TRY(cudaMalloc(&r->d_flush, sizeof(double) * n));
+        r->flush_n = n;
+    }
+    CUDA_TRY(launch_flush(r->d_flush, n, r->stream));
+    r->prof.launches += 1;
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return VOCE_OK;
+}
+
+void *voce_host_alloc(long long bytes)
+{
+    void *p = nullptr;
+    if (bytes <= 0 || cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void voce_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}
+
+double voce_measure_fp64_tflops(void) { return measure_fp64_tflops(); }
+
+}  // extern "C"

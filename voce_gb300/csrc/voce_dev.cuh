@@ -1,0 +1,439 @@
+// Device-side data structures and math of the GB300 EVP-FFT solver step.
+//
+// Layout in HBM (one RVE, nv = nx*ny*nz voxels, x slowest / z fastest, SoA):
+//   sig[6][nv]    stress in the Lebensohn-Tome 6-vector basis (the basis of
+//                 the reference's chg_basis, kinematics.c:14-174)
+//   sigp[5][nv]   stress before the last Newton update (the point at which
+//                 the reference evaluates Edot/gamdot, evolution.c:67,126)
+//   eps[5][nv]    total strain at time t in the same basis (6th comp is 0)
+//   dgs[6][nv]    symmetric part of the displacement gradient, same basis
+//   dga[3][nv]    antisymmetric part: (D12-D21)/2, (D02-D20)/2, (D01-D10)/2
+//   tm[9][nv]     crystal->sample rotation TranMat_xt2sa (evp.h:240)
+//   sch[60][nv]   Schmid 5-vectors of the 12 systems in sample axes
+//   sg[21][nv]    grain compliance S_g = C_gr^-1, packed upper triangle
+//   crss[24][nv]  critical resolved shear stress (system, +/- direction)
+//   itau[24][nv]  1/crss
+//   gamacum[nv], gtot[12][nv], edot[5][nv], gamdot[12][nv], taux[12][nv],
+//   svm[nv], evm[nv], phase[nv]
+//   spec[6][nzh][nx][ny] half spectrum (kz = 0..nz/2), complex, y fastest
+//   aacc[3][nzh][nx][ny] antisymmetric part of the Green update, summed
+//                 over the iterations of the current increment
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define VOCE_NS 12
+#define VOCE_NPART 16
+#define VOCE_MAXRAD 12
+#define VOCE_ITLOG 12   // doubles per logged iteration
+
+// Lebensohn-Tome basis constants, the literal values of kinematics.c:333-335
+#define RSQ2 0.70710678118654744
+#define RSQ3 0.57735026918962584
+#define RSQ6 0.40824829046386304
+#define VOCE_PI_REF 3.14159265359
+#define VOCE_TWO_PI_REF 6.28318530718
+
+struct FftPlan1 {
+    int L, nst;
+    int rad[VOCE_MAXRAD];
+};
+
+// Per-RVE macro state (device, written only by the single-thread
+// finalisers).  Mirrors the reference's macro globals and Evolution locals.
+struct MacroDev {
+    double DisGradAvg[9], DisGradAvg_t[9], DisGradAvg_actual[9];
+    double dDisGradAvg[9], dDisGradAvg_acum[9], VelGradAvg[9], DGA_prev[9];
+    double SigAvg[9], SigAvg1[9], EpsAvg[9], EdotAvg[9];
+    double s_vm, s_vm1, e_vm, d_vm, evmp, dvmp, Err_e, Err_s;
+    double ddg6[6];      // B-basis sym(dDisGradAvg) used by the next c2r update
+    double acum_a[3];    // antisym(dDisGradAvg_acum): A12, A02, A01
+    double rsl, rlc, nr_total;
+    int iter, iter_total, istep, converged, nr_max, first_iter, done;
+    int pad;
+};
+
+// Per-increment record (device array, one per increment run)
+struct IncrDev {
+    int istep, iters, iter_total, nr_max;
+    double e_vm, evmp, d_vm, dvmp, s_vm, s_vm1;
+    double sig_avg[9], sig_avg1[9], eps_avg[9], edot_avg[9], disgrad_avg[9];
+    double err_e, err_s, rsl, rlc, nr_total;
+};
+
+// Everything a kernel needs to know about one RVE.  Passed by value as a
+// kernel parameter (it is ~3 KB; the limit is 32 KB).
+struct RveDesc {
+    int nx, ny, nz, nzh;
+    long long nv, nspec;
+    int solid[3];        // solid[phase id 1..2]
+    int nsys, ipow_n;    // ipow_n >= 0: n integral, |r|^(n-1) by multiplication
+    int update_flag, hard_flag, creep, iter_max;
+    int mixed;           // spectrum precision: 0 double, 1 float
+    double dt, wgt, wgt_ph1, err_tol, inv_nv;
+    double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
+    double tau0[VOCE_NS], tau1[VOCE_NS], thet0[VOCE_NS], thet1[VOCE_NS];
+    double hard[VOCE_NS * VOCE_NS];
+    double bn[VOCE_NS * 3], bb[VOCE_NS * 3];
+    double S0[36];       // S066 (B basis)
+    double S0t[81];      // S0 as 3x3x3x3 (get_smacro's dDisGradAvg)
+    double Kq[36];       // acoustic tensor coefficients: K6 = Kq * nn6
+    double Udot[9], Scauchy[9];
+    double u6[6];        // B-basis sym(Udot)
+    double ua[3];        // antisym(Udot): A12, A02, A01
+    int vflag[6], sflag[6];
+    FftPlan1 plx, ply, plz;
+    // fields
+    double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
+    double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl;
+    int *phase;
+    void *spec, *aacc;
+    const void *twx, *twy, *twz;  // exp(-2 pi i j / L), complex of the spectrum type
+    double *part;        // [npart_blocks][VOCE_NPART]
+    int npart;
+    MacroDev *macro;
+    double *itlog;       // [iter_max][VOCE_ITLOG] for the current increment
+    IncrDev *incr;       // [capacity]
+    int incr_cap;
+};
+
+// ---------------------------------------------------------------------------
+// small tensor helpers.  Symmetric 3x3 as 6 comps (00,11,22,12,02,01).
+// ---------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ __forceinline__ void t6_to_b(const T *t, T *b)
+{
+    b[0] = T(RSQ2) * (t[1] - t[0]);
+    b[1] = T(RSQ6) * (T(2) * t[2] - t[0] - t[1]);
+    b[2] = T(2.0 * RSQ2) * t[3];
+    b[3] = T(2.0 * RSQ2) * t[4];
+    b[4] = T(2.0 * RSQ2) * t[5];
+    b[5] = T(RSQ3) * (t[0] + t[1] + t[2]);
+}
+
+template <typename T>
+__host__ __device__ __forceinline__ void b_to_t6(const T *b, T *t)
+{
+    t[0] = -T(RSQ2) * b[0] - T(RSQ6) * b[1] + T(RSQ3) * b[5];
+    t[1] = T(RSQ2) * b[0] - T(RSQ6) * b[1] + T(RSQ3) * b[5];
+    t[2] = T(2.0 * RSQ6) * b[1] + T(RSQ3) * b[5];
+    t[3] = T(RSQ2) * b[2];
+    t[4] = T(RSQ2) * b[3];
+    t[5] = T(RSQ2) * b[4];
+}
+
+// packed upper-triangle index of a symmetric 6x6
+__host__ __device__ __forceinline__ int sym6(int i, int j)
+{
+    int a = i < j ? i : j, b = i < j ? j : i;
+    return a * 6 - (a * (a - 1)) / 2 + (b - a);
+}
+
+// Newton-Raphson reciprocal: a single-precision seed refined by three steps
+// of r <- r + r(1 - x r) (each step squares the relative error:
+// 2^-23 -> 2^-46 -> 2^-92), falling back to division outside the range
+// where the float seed is meaningful.
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    double ax = fabs(x);
+    if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
+    double r = (double)(1.0f / (float)x);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    return r;
+}
+
+// |r|^e by binary powering (e >= 0), exact integer exponent
+__device__ __forceinline__ double ipow_abs(double a, int e)
+{
+    double res = 1.0, b = a;
+    while (e) {
+        if (e & 1) res *= b;
+        e >>= 1;
+        if (e) b *= b;
+    }
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Flow rule: StrainRate_eval (constitutive.c:126-194) on a stress 5-vector.
+// edot[5] = sum_k sch_k * gdot_k; D (packed 15, 5x5 sym) = sum_k rss1_k sch_k sch_k^T
+// xkin is always zero in the reference (init.c:793) and is left out.
+// ---------------------------------------------------------------------------
+template <bool WANT_D, bool WANT_SYS>
+__device__ __forceinline__ void flow_rule(const RveDesc &d, long long v, const double *s,
+                                          double *edot, double *D, double *gd, double *tx)
+{
+    const long long nv = d.nv;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) edot[i] = 0.0;
+    if (WANT_D) {
+#pragma unroll
+        for (int i = 0; i < 15; ++i) D[i] = 0.0;
+    }
+    for (int k = 0; k < d.nsys; ++k) {
+        double sc[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
+        double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        int neg = rss < 0.0;
+        double it = __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
+        double r = rss * it;
+        double ap;
+        if (d.ipow_n >= 1) ap = ipow_abs(fabs(r), d.ipow_n - 1);
+        else ap = fabs(pow(r, d.nrs[k] - 1.0));
+        double g1 = d.g0n[k] * ap * it;                      // rss1 = gam0 n |r^(n-1)| / tau
+        double an = (d.ipow_n >= 1) ? ap * fabs(r) : fabs(pow(r, d.nrs[k]));
+        double g2 = d.gam0[k] * an * (r > 0.0 ? 1.0 : -1.0);  // rss2 = gam0 |r^n| sign(r)
+        if (WANT_SYS) { gd[k] = g2; tx[k] = g1; }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) edot[i] = fma(sc[i], g2, edot[i]);
+        if (WANT_D) {
+            double t[5];
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = g1 * sc[i];
+            int q = 0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+#pragma unroll
+                for (int j = i; j < 5; ++j) { D[q] = fma(t[i], sc[j], D[q]); ++q; }
+        }
+    }
+}
+
+// Solve M x = b for symmetric positive definite M (6x6, full storage, only
+// the lower triangle read) by an LDL^T factorisation without pivoting.
+__device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)[6])
+{
+    double L[6][6], w[6][6], dinv[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        double dj = M[j][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) dj = fma(-L[j][k], w[j][k], dj);
+        dinv[j] = rcp_nr(dj);
+#pragma unroll
+        for (int i = j + 1; i < 6; ++i) {
+            double s = M[i][j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) s = fma(-L[i][k], w[j][k], s);
+            w[i][j] = s;
+            L[i][j] = s * dinv[j];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        double s = b[i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) s = fma(-L[i][k], b[k], s);
+        b[i] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) b[i] *= dinv[i];
+#pragma unroll
+    for (int i = 5; i >= 0; --i) {
+        double s = b[i];
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) s = fma(-L[k][i], b[k], s);
+        b[i] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Green operator on the fly.  The reference tabulates
+//   Gamma_ijkl(k) = -omega_ik n_j n_l,  omega = (C0_ijkl n_j n_l)^-1
+// per frequency (init.c:546-615) and contracts it with the stress spectrum
+// (evolution.c:363-377).  Here, per frequency: t = sig^ n, v = omega t,
+// dU = -v (x) n, split into its symmetric part (6 comps, basis B) and its
+// antisymmetric part (A12, A02, A01).
+// The reference takes the real part of a complex inverse FFT of dU
+// (evolution.c:389-392); that equals the inverse transform of the Hermitian
+// part of dU, i.e. of (Gamma(k) + Gamma(-k))/2 applied to sig^(k).  Gamma is
+// even in n except on the Nyquist planes, where n(-k) is not -n(k) because
+// the reference maps index N/2 to -pi for both k and -k (init.c:661-666);
+// there both operators are applied and averaged.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double kfreq(int i, int n)
+{
+    double t = (double)i * (double)(1.0 / n);
+    t -= round(t);
+    return t * VOCE_TWO_PI_REF;
+}
+
+__device__ __forceinline__ void unit_freq(int ix, int iy, int iz, int nx, int ny, int nz, double *n)
+{
+    double g0 = kfreq(ix, nx), g1 = kfreq(iy, ny), g2 = kfreq(iz, nz);
+    double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+    double s = 1.0 / gn;
+    n[0] = g0 * s; n[1] = g1 * s; n[2] = g2 * s;
+}
+
+template <typename R>
+__device__ __forceinline__ void green_rank1(const double *Kq, const double *nd,
+                                            const R (&sr)[6], const R (&si)[6],
+                                            R (&ur)[6], R (&ui)[6], R (&ar)[3], R (&ai)[3],
+                                            R wgt)
+{
+    // acoustic tensor K_ik = C0_ijkl n_j n_l (6 sym comps) = Kq * nn
+    double nn[6] = {nd[0] * nd[0], nd[1] * nd[1], nd[2] * nd[2],
+                    nd[1] * nd[2], nd[0] * nd[2], nd[0] * nd[1]};
+    double K[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        double s = 0.0;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) s = fma(Kq[a * 6 + m], nn[m], s);
+        K[a] = s;
+    }
+    // omega = K^-1 by cofactors (M3Inverse, init.c:546-568); K symmetric
+    double c00 = K[1] * K[2] - K[3] * K[3];
+    double c01 = K[4] * K[3] - K[5] * K[2];
+    double c02 = K[5] * K[3] - K[4] * K[1];
+    double c11 = K[0] * K[2] - K[4] * K[4];
+    double c12 = K[4] * K[5] - K[0] * K[3];
+    double c22 = K[0] * K[1] - K[5] * K[5];
+    double det = K[0] * c00 + K[5] * c01 + K[4] * c02;
+    double id = 1.0 / det;
+    R w00 = R(c00 * id), w01 = R(c01 * id), w02 = R(c02 * id);
+    R w11 = R(c11 * id), w12 = R(c12 * id), w22 = R(c22 * id);
+    R n0 = R(nd[0]), n1 = R(nd[1]), n2 = R(nd[2]);
+    // t = sig^ n (sig^ symmetric: 00,11,22,12,02,01)
+    R t0r = sr[0] * n0 + sr[5] * n1 + sr[4] * n2, t0i = si[0] * n0 + si[5] * n1 + si[4] * n2;
+    R t1r = sr[5] * n0 + sr[1] * n1 + sr[3] * n2, t1i = si[5] * n0 + si[1] * n1 + si[3] * n2;
+    R t2r = sr[4] * n0 + sr[3] * n1 + sr[2] * n2, t2i = si[4] * n0 + si[3] * n1 + si[2] * n2;
+    R v0r = w00 * t0r + w01 * t1r + w02 * t2r, v0i = w00 * t0i + w01 * t1i + w02 * t2i;
+    R v1r = w01 * t0r + w11 * t1r + w12 * t2r, v1i = w01 * t0i + w11 * t1i + w12 * t2i;
+    R v2r = w02 * t0r + w12 * t1r + w22 * t2r, v2i = w02 * t0i + w12 * t1i + w22 * t2i;
+    // dU = -v (x) n ; weight wgt (1 or 1/2 on the Nyquist planes)
+    R h = -wgt;
+    R hh = R(0.5) * h;
+    ur[0] += h * v0r * n0;                 ui[0] += h * v0i * n0;
+    ur[1] += h * v1r * n1;                 ui[1] += h * v1i * n1;
+    ur[2] += h * v2r * n2;                 ui[2] += h * v2i * n2;
+    ur[3] += hh * (v1r * n2 + v2r * n1);   ui[3] += hh * (v1i * n2 + v2i * n1);
+    ur[4] += hh * (v0r * n2 + v2r * n0);   ui[4] += hh * (v0i * n2 + v2i * n0);
+    ur[5] += hh * (v0r * n1 + v1r * n0);   ui[5] += hh * (v0i * n1 + v1i * n0);
+    ar[0] += hh * (v1r * n2 - v2r * n1);   ai[0] += hh * (v1i * n2 - v2i * n1);
+    ar[1] += hh * (v0r * n2 - v2r * n0);   ai[1] += hh * (v0i * n2 - v2i * n0);
+    ar[2] += hh * (v0r * n1 - v1r * n0);   ai[2] += hh * (v0i * n1 - v1i * n0);
+}
+
+// Apply the Green operator at frequency (ix,iy,iz).  In: B-basis stress
+// spectrum (br, bi).  Out: B-basis symmetric update in (br, bi) and the
+// antisymmetric update (ar, ai).
+template <typename R>
+__device__ __forceinline__ void green_apply(const RveDesc &d, int ix, int iy, int iz,
+                                            R (&br)[6], R (&bi)[6], R (&ar)[3], R (&ai)[3])
+{
+    R sr[6], si[6], ur[6], ui[6];
+    b_to_t6<R>(br, sr);
+    b_to_t6<R>(bi, si);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) { ur[a] = R(0); ui[a] = R(0); }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { ar[a] = R(0); ai[a] = R(0); }
+    if ((ix | iy | iz) != 0) {
+        double n[3];
+        unit_freq(ix, iy, iz, d.nx, d.ny, d.nz, n);
+        bool nyq = ((d.nx % 2 == 0) && ix == d.nx / 2) || ((d.ny % 2 == 0) && iy == d.ny / 2) ||
+                   ((d.nz % 2 == 0) && iz == d.nz / 2);
+        if (!nyq) {
+            green_rank1<R>(d.Kq, n, sr, si, ur, ui, ar, ai, R(1));
+        } else {
+            double n2[3];
+            unit_freq((d.nx - ix) % d.nx, (d.ny - iy) % d.ny, (d.nz - iz) % d.nz, d.nx, d.ny, d.nz, n2);
+            green_rank1<R>(d.Kq, n, sr, si, ur, ui, ar, ai, R(0.5));
+            green_rank1<R>(d.Kq, n2, sr, si, ur, ui, ar, ai, R(0.5));
+        }
+    }
+    t6_to_b<R>(ur, br);
+    t6_to_b<R>(ui, bi);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory Stockham FFT over NL lines of length L.  Element (line l,
+// index i) lives at buf[i * ldl + l].  sign -1: exp(-2 pi i jk/L) (forward),
+// +1: inverse; unnormalised.  Returns the buffer holding the result.
+// ---------------------------------------------------------------------------
+template <typename R> struct Cx;
+template <> struct Cx<double> { typedef double2 T; };
+template <> struct Cx<float> { typedef float2 T; };
+
+template <typename R>
+__device__ __forceinline__ typename Cx<R>::T cmul(typename Cx<R>::T a, typename Cx<R>::T b)
+{
+    typename Cx<R>::T c;
+    c.x = a.x * b.x - a.y * b.y;
+    c.y = a.x * b.y + a.y * b.x;
+    return c;
+}
+
+template <typename R>
+__device__ typename Cx<R>::T *fft_lines(typename Cx<R>::T *a, typename Cx<R>::T *b, int NL,
+                                        int ldl, const FftPlan1 &pl,
+                                        const typename Cx<R>::T *__restrict__ tw, int sign)
+{
+    typedef typename Cx<R>::T C;
+    const int L = pl.L;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    int ncur = L, s = 1;
+    C *src = a, *dst = b;
+    const R sg = R(sign);
+    for (int st = 0; st < pl.nst; ++st) {
+        const int r = pl.rad[st];
+        const int m = ncur / r;
+        const int nb = NL * (L / r);
+        for (int bi = tid; bi < nb; bi += nthr) {
+            const int l = bi % NL;
+            const int t = bi / NL;
+            const int p = t / s, q = t - (t / s) * s;
+            C x[4], y[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < r) x[j] = src[(q + s * (p + j * m)) * ldl + l];
+            if (r == 4) {
+                C t0, t1, t2, t3;
+                t0.x = x[0].x + x[2].x; t0.y = x[0].y + x[2].y;
+                t1.x = x[0].x - x[2].x; t1.y = x[0].y - x[2].y;
+                t2.x = x[1].x + x[3].x; t2.y = x[1].y + x[3].y;
+                t3.x = x[1].x - x[3].x; t3.y = x[1].y - x[3].y;
+                y[0].x = t0.x + t2.x;       y[0].y = t0.y + t2.y;
+                y[2].x = t0.x - t2.x;       y[2].y = t0.y - t2.y;
+                y[1].x = t1.x - sg * t3.y;  y[1].y = t1.y + sg * t3.x;
+                y[3].x = t1.x + sg * t3.y;  y[3].y = t1.y - sg * t3.x;
+            } else if (r == 2) {
+                y[0].x = x[0].x + x[1].x; y[0].y = x[0].y + x[1].y;
+                y[1].x = x[0].x - x[1].x; y[1].y = x[0].y - x[1].y;
+            } else {  // r == 3
+                const R c3 = R(-0.5), s3 = sg * R(0.86602540378443864676);
+                C u;
+                u.x = x[1].x + x[2].x; u.y = x[1].y + x[2].y;
+                C w;
+                w.x = x[1].x - x[2].x; w.y = x[1].y - x[2].y;
+                y[0].x = x[0].x + u.x; y[0].y = x[0].y + u.y;
+                C m0;
+                m0.x = x[0].x + c3 * u.x; m0.y = x[0].y + c3 * u.y;
+                y[1].x = m0.x - s3 * w.y; y[1].y = m0.y + s3 * w.x;
+                y[2].x = m0.x + s3 * w.y; y[2].y = m0.y - s3 * w.x;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k >= r) break;
+                const int e = p * k * s;  // < L
+                C w = tw[e];
+                if (sign > 0) w.y = -w.y;
+                C z = (e == 0) ? y[k] : cmul<R>(y[k], w);
+                dst[(q + s * (r * p + k)) * ldl + l] = z;
+            }
+        }
+        __syncthreads();
+        ncur = m;
+        s *= r;
+        C *tt = src; src = dst; dst = tt;
+    }
+    return src;
+}

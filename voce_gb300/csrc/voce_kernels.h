@@ -1,0 +1,67 @@
+// Host-side declarations of the kernel launchers (voce_kernels.cu).
+#pragma once
+#include "voce_dev.cuh"
+
+namespace voce {
+
+// Constants used only by the setup and increment-end kernels.
+struct SetupConst {
+    double cxt[36], sxt[36];  // crystal stiffness / compliance, 6-vector basis
+    double d6[6];             // B-basis sym(DisGradAvg) at t=0 (init.c:495-499)
+    double sc6[6];            // B-basis Scauchy (creep start stress, init.c:523-525)
+    double tau0b[VOCE_NS];    // backward CRSS start value
+    double schxt[VOCE_NS * 5];  // Schmid 5-vectors in crystal axes
+};
+
+// FFT tile sizes (lines per block) for one grid
+struct Tiles {
+    int zrows, yxt, xkc, xkc3, zirows, zirows3;
+    template <typename R> void choose(const RveDesc &d);
+};
+
+// Per-kernel timing: when `on`, an event pair brackets every launch of the
+// listed kernels; the host reads them after the stream synchronises.
+enum KernelId {
+    K_FFT_Z_FWD = 0, K_FFT_Y_FWD, K_FFT_X_GREEN, K_FFT_Y_INV, K_FFT_Z_INV, K_NR, K_FIN_ITER,
+    K_PRELUDE, K_INC_FFT, K_INCR_END, K_FIN_INCR, K_COUNT
+};
+struct Prof {
+    bool on = false;
+    cudaEvent_t ev[2 * K_COUNT] = {};
+    bool pending[K_COUNT] = {};
+    double ms[K_COUNT] = {};
+    long long n[K_COUNT] = {};
+    long long launches = 0;   // kernels issued, counted whether or not timing is on
+    void begin(int k, cudaStream_t s) { if (on) cudaEventRecord(ev[2 * k], s); }
+    void end(int k, cudaStream_t s, int count = 1)
+    {
+        launches += count;
+        if (on) { cudaEventRecord(ev[2 * k + 1], s); pending[k] = true; }
+    }
+    void collect()   // after a stream synchronisation
+    {
+        for (int k = 0; k < K_COUNT; ++k)
+            if (pending[k]) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]);
+                ms[k] += t;
+                n[k] += 1;
+                pending[k] = false;
+            }
+    }
+};
+
+template <typename R>
+cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf);
+template <typename R>
+cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,
+                                 cudaStream_t s, Prof &pf);
+cudaError_t set_smem_limits(bool mixed, const Tiles &t, const RveDesc &d);
+cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
+double measure_fp64_tflops();
+cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
+                         cudaStream_t s);
+cudaError_t launch_prelude(const RveDesc &d, cudaStream_t s, Prof &pf);
+cudaError_t launch_field_out(const RveDesc &d, int field, double *out, cudaStream_t s);
+
+}  // namespace voce

@@ -90,8 +90,11 @@ def random_traceless_load(rng: np.random.Generator, rate: float = 1e-3) -> Load:
     s = 0.5 * (a + a.T)
     s -= np.eye(3) * np.trace(s) / 3.0
     s *= rate / np.linalg.norm(s)
-    v = (s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1])
-    return Load((1,) * 6, tuple(float(x) for x in v), (0,) * 6)
+    # quantised to 1e-6 so that a namelist line fits the reader's 80 bytes;
+    # L33 is set so that the trace stays zero after rounding
+    v = [round(float(x), 6) for x in (s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1])]
+    v[2] = round(-(v[0] + v[1]), 6)
+    return Load((1,) * 6, tuple(v), (0,) * 6)
 
 
 @dataclasses.dataclass
@@ -221,14 +224,14 @@ def write_namelist(path: str, dims, mat: Material, load: Load, *,
     ``Hirth`` -- the capitalisation the reference's own example input uses
     (input:86) -- which the case-sensitive parser ignores, so the effective
     Hirth coefficient is 0, exactly as in the reference."""
-    f6 = lambda v: " ".join("%.17g" % x for x in v)
+    f6 = lambda v: " ".join(repr(float(x)) for x in v)   # shortest round trip
     i6 = lambda v: " ".join("%d" % x for x in v)
     L = [
         "# generated", "N_phases\t%d" % n_phases,
         "CellDim\t\t%d %d %d" % tuple(dims),
         "initial_ms\t\t%s" % mesh_name,
         "Type_phases\t\t0  1",
-        "ElastConst_PhaseI\t%.17g %.17g %.17g %.17g" % (mat.c11, mat.c12, mat.c44, mat.nu),
+        "ElastConst_PhaseI\t%s" % f6((mat.c11, mat.c12, mat.c44, mat.nu)),
         "Slip_PhaseI\t\t%s" % sx_name,
         "ElastConst_PhaseII\t0.0 0.0 0.0 0.0",
         "Slip_PhaseII\tXXXXX",
@@ -236,9 +239,9 @@ def write_namelist(path: str, dims, mat: Material, load: Load, *,
         "VelGrad_BC\t\t%s" % f6(load.velgrad),
         "Stress_BC_Flag\t\t%s" % i6(load.stress_flag),
         "Stress_BC\t%s" % f6(load.stress),
-        "TimeStep\t%.17g" % time_step,
+        "TimeStep\t%r" % float(time_step),
         "N_steps\t\t%d" % n_steps,
-        "Err\t\t%.17g" % err,
+        "Err\t\t%r" % float(err),
         "IterMax\t\t%d" % iter_max,
         "PrintControl\t%d\t%d" % tuple(print_control),
         "Update_Flag\t\t%d" % update_flag,
@@ -246,7 +249,7 @@ def write_namelist(path: str, dims, mat: Material, load: Load, *,
         "Tex_Flag\t\t%d" % tex_flag,
     ]
     for k in ("self", "coplane", "cross", "glissile", "Hirth", "lomer"):
-        L.append("%s\t%.17g\t0.0" % (k, mat.latent[k]))
+        L.append("%s\t%r\t0.0" % (k, float(mat.latent[k])))
     for s in L:
         assert len(s) < 79, s
     with open(path, "w") as f:
