@@ -32,8 +32,13 @@ enum {
 /* voce_rve_run bracketed by CUDA events on the RVE's stream; device_ms is
  * the elapsed time between them. */
 int voce_rve_run_timed(voce_rve *r, int n_increments, double *device_ms);
+/* Execution strategy of voce_rve_run: 1 (default) runs each increment as one
+ * CUDA graph whose Green-iteration loop is a device-side conditional WHILE
+ * node; 0 lets the host read the convergence flag after every iteration.
+ * Results are identical. */
+int voce_rve_set_graph(voce_rve *r, int on);
 /* When on, every kernel launch is bracketed by an event pair; the totals
- * accumulate until reset. */
+ * accumulate until reset.  Profiling runs the host-driven loop. */
 int voce_rve_set_profiling(voce_rve *r, int on);
 int voce_rve_get_kernel_time(const voce_rve *r, int kernel, double *ms_total,
                              long long *timed_launches);

@@ -100,6 +100,7 @@ PROTOTYPES = [
     ("voce_rve_footprint", C.c_longlong, [C.POINTER(C.c_int), C.c_int]),
     # voce_gpu_diag.h
     ("voce_rve_run_timed", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_rve_set_graph", C.c_int, [C.c_void_p, C.c_int]),
     ("voce_rve_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("voce_rve_get_kernel_time", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                            C.POINTER(C.c_longlong)]),
@@ -240,6 +241,9 @@ class Rve:
         ms = C.c_double()
         _check(load().voce_rve_run_timed(self._h, n, C.byref(ms)))
         return ms.value
+
+    def set_graph(self, on: bool) -> None:
+        _check(load().voce_rve_set_graph(self._h, int(on)))
 
     def set_profiling(self, on: bool) -> None:
         _check(load().voce_rve_set_profiling(self._h, int(on)))

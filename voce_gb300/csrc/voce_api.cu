@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -185,12 +186,17 @@ struct voce_rve {
     double *d_flush = nullptr;
     long long flush_n = 0;
     Prof prof;
+    bool use_graph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
     int n_done = 0, n_steps = 0;
     std::vector<voce_increment> incr;
     std::vector<std::vector<double>> itlog;
     ~voce_rve()
     {
         if (stream) cudaStreamSynchronize(stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
         for (void *p : dev_allocs) cudaFree(p);
         if (d_out) cudaFree(d_out);
         if (d_flush) cudaFree(d_flush);
@@ -385,7 +391,7 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3  (= 211) + phase (4 bytes)
-    return nv * (211 * 8 + 4) + nspec * 9 * cplx;
+    return nv * (211 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 240 : 0)) + nspec * 9 * cplx;
 }
 
 // ---------------------------------------------------------------------------
@@ -546,11 +552,13 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     AL(d.tm, 9 * nv); AL(d.sch, 60 * nv); AL(d.sg, 21 * nv); AL(d.crss, 24 * nv); AL(d.itau, 24 * nv);
     AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
     AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.phase, nv);
+    d.sch32 = nullptr;
+    if (r->precision) AL(d.sch32, 60 * nv);
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
     AL(d.macro, 1);
-    AL(d.itlog, (size_t)VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
-    d.incr_cap = 1;
-    AL(d.incr, 1);
+    d.incr_cap = 32;   // increments per host read-back
+    AL(d.itlog, (size_t)d.incr_cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
+    AL(d.incr, d.incr_cap);
     const size_t csz = r->precision ? sizeof(float2) : sizeof(double2);
     {
         char *p;
@@ -677,54 +685,137 @@ int voce_rve_create_from_files(const char *namelist_path, int precision, voce_rv
 // ---------------------------------------------------------------------------
 // Evolution (evolution.c:265-622), n increments at a time
 // ---------------------------------------------------------------------------
+namespace {
+
+// Record of one finished increment, copied from the device rings.
+void collect_increment(voce_rve *r, const IncrDev &rec, const double *log_rows)
+{
+    voce_increment o;
+    std::memset(&o, 0, sizeof(o));
+    o.istep = rec.istep; o.iters = rec.iters; o.iter_total = rec.iter_total; o.nr_max = rec.nr_max;
+    o.e_vm = rec.e_vm; o.evmp = rec.evmp; o.d_vm = rec.d_vm; o.dvmp = rec.dvmp;
+    o.s_vm = rec.s_vm; o.s_vm1 = rec.s_vm1;
+    std::memcpy(o.sig_avg, rec.sig_avg, sizeof(o.sig_avg));
+    std::memcpy(o.sig_avg1, rec.sig_avg1, sizeof(o.sig_avg1));
+    std::memcpy(o.eps_avg, rec.eps_avg, sizeof(o.eps_avg));
+    std::memcpy(o.edot_avg, rec.edot_avg, sizeof(o.edot_avg));
+    std::memcpy(o.disgrad_avg, rec.disgrad_avg, sizeof(o.disgrad_avg));
+    o.err_e = rec.err_e; o.err_s = rec.err_s;
+    o.rot_slip_avg = rec.rsl; o.rot_loc_avg = rec.rlc;
+    o.nr_iters_total = rec.nr_total;
+    r->incr.push_back(o);
+    r->itlog.emplace_back(log_rows, log_rows + (size_t)VOCE_ITLOG * rec.iters);
+    r->n_done++;
+}
+
+// One increment with the host deciding after every iteration (used when
+// profiling per kernel, and when the loop bounds are degenerate).
+int run_increment_hostloop(voce_rve *r)
+{
+    RveDesc &d = r->d;
+    CUDA_TRY(launch_prelude(d, r->stream, r->prof));
+    int guard = 0;
+    // the reference tests the loop condition before the first iteration
+    const bool any = d.iter_max > 0 && 2.0 * std::fabs(d.err_tol) > std::fabs(d.err_tol);
+    while (any) {
+        cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, r->prof)
+                                     : launch_iteration<double>(d, r->tiles, r->npart, r->stream, r->prof);
+        if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "iteration launch: %s", cudaGetErrorString(e));
+        CUDA_TRY(cudaMemcpyAsync(r->h_flag, &d.macro->converged, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        r->prof.collect();
+        if (*r->h_flag) break;
+        if (++guard > d.iter_max + 1) return fail(VOCE_ERR_STATE, "iteration control lost");
+    }
+    cudaError_t e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, r->prof)
+                                 : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, r->prof);
+    if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "increment-end launch: %s", cudaGetErrorString(e));
+    return VOCE_OK;
+}
+
+// The increment as one CUDA graph: prelude, a conditional WHILE node whose
+// body is one Green-operator iteration (the finaliser sets the condition),
+// then the increment end.  Built on first use; kernel arguments do not
+// change between launches, all state lives in device memory.
+int build_graph(voce_rve *r)
+{
+    RveDesc &d = r->d;
+    Prof none;  // no events inside graphs
+    cudaGraph_t g;
+    CUDA_TRY(cudaGraphCreate(&g, 0));
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    CUDA_TRY(launch_prelude(d, r->stream, none));
+    CUDA_TRY(cudaStreamEndCapture(r->stream, &g));
+    size_t nn = 0;
+    CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> pre(nn);
+    CUDA_TRY(cudaGraphGetNodes(g, pre.data(), &nn));
+    cudaGraphConditionalHandle h;
+    CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond;
+    CUDA_TRY(cudaGraphAddNode(&cond, g, pre.data(), nullptr, pre.size(), &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, none, h, 1)
+                                 : launch_iteration<double>(d, r->tiles, r->npart, r->stream, none, h, 1);
+    CUDA_TRY(cudaStreamEndCapture(r->stream, &body));
+    CUDA_TRY(e);
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, g, &cond, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+    e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, none)
+                     : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, none);
+    CUDA_TRY(cudaStreamEndCapture(r->stream, &g));
+    CUDA_TRY(e);
+    CUDA_TRY(cudaGraphInstantiate(&r->graph_exec, g, 0));
+    r->graph = g;
+    // launches per increment: prelude + 7 per iteration + 5 at the end
+    return VOCE_OK;
+}
+
+}  // namespace
+
 int voce_rve_run(voce_rve *r, int n)
 {
     if (!r || n < 0) return fail(VOCE_ERR_ARG, "bad argument");
     RveDesc &d = r->d;
-    for (int k = 0; k < n; ++k) {
-        CUDA_TRY(launch_prelude(d, r->stream, r->prof));
-        int guard = 0;
-        while (true) {
-            cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, r->prof)
-                                         : launch_iteration<double>(d, r->tiles, r->npart, r->stream, r->prof);
-            if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "iteration launch: %s", cudaGetErrorString(e));
-            CUDA_TRY(cudaMemcpyAsync(r->h_flag, &d.macro->converged, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
-            CUDA_TRY(cudaStreamSynchronize(r->stream));
-            r->prof.collect();
-            if (*r->h_flag) break;
-            if (++guard > d.iter_max + 1) return fail(VOCE_ERR_STATE, "iteration control lost");
+    const bool graph_ok = r->use_graph && !r->prof.on && d.iter_max > 0 && d.err_tol != 0.0;
+    if (graph_ok && !r->graph_exec) {
+        int rc = build_graph(r);
+        if (rc) return rc;
+    }
+    int done = 0;
+    while (done < n) {
+        const int chunk = std::min(n - done, d.incr_cap);
+        const int first = r->n_done;
+        for (int k = 0; k < chunk; ++k) {
+            if (graph_ok) {
+                CUDA_TRY(cudaGraphLaunch(r->graph_exec, r->stream));
+            } else {
+                int rc = run_increment_hostloop(r);
+                if (rc) return rc;
+            }
         }
-        // copy the iteration log before the increment end resets the counters
-        MacroDev m;
-        CUDA_TRY(cudaMemcpyAsync(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost, r->stream));
+        // records and iteration logs of the chunk (device rings of incr_cap)
+        std::vector<IncrDev> recs(d.incr_cap);
+        std::vector<double> logs((size_t)d.incr_cap * d.iter_max * VOCE_ITLOG);
+        CUDA_TRY(cudaMemcpyAsync(recs.data(), d.incr, sizeof(IncrDev) * recs.size(), cudaMemcpyDeviceToHost, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(logs.data(), d.itlog, sizeof(double) * logs.size(), cudaMemcpyDeviceToHost, r->stream));
         CUDA_TRY(cudaStreamSynchronize(r->stream));
-        std::vector<double> log((size_t)VOCE_ITLOG * m.iter);
-        if (m.iter)
-            CUDA_TRY(cudaMemcpyAsync(log.data(), d.itlog, sizeof(double) * log.size(), cudaMemcpyDeviceToHost, r->stream));
-        cudaError_t e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, r->prof)
-                                     : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, r->prof);
-        if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "increment-end launch: %s", cudaGetErrorString(e));
-        IncrDev rec;
-        CUDA_TRY(cudaMemcpyAsync(&rec, d.incr, sizeof(rec), cudaMemcpyDeviceToHost, r->stream));
-        CUDA_TRY(cudaStreamSynchronize(r->stream));
-        r->prof.collect();
-        // one record slot, reused every increment (incr_cap == 1)
-        voce_increment o;
-        std::memset(&o, 0, sizeof(o));
-        o.istep = rec.istep; o.iters = rec.iters; o.iter_total = rec.iter_total; o.nr_max = rec.nr_max;
-        o.e_vm = rec.e_vm; o.evmp = rec.evmp; o.d_vm = rec.d_vm; o.dvmp = rec.dvmp;
-        o.s_vm = rec.s_vm; o.s_vm1 = rec.s_vm1;
-        std::memcpy(o.sig_avg, rec.sig_avg, sizeof(o.sig_avg));
-        std::memcpy(o.sig_avg1, rec.sig_avg1, sizeof(o.sig_avg1));
-        std::memcpy(o.eps_avg, rec.eps_avg, sizeof(o.eps_avg));
-        std::memcpy(o.edot_avg, rec.edot_avg, sizeof(o.edot_avg));
-        std::memcpy(o.disgrad_avg, rec.disgrad_avg, sizeof(o.disgrad_avg));
-        o.err_e = rec.err_e; o.err_s = rec.err_s;
-        o.rot_slip_avg = rec.rsl; o.rot_loc_avg = rec.rlc;
-        o.nr_iters_total = rec.nr_total;
-        r->incr.push_back(o);
-        r->itlog.push_back(std::move(log));
-        r->n_done++;
+        CUDA_TRY(cudaGetLastError());
+        for (int k = 0; k < chunk; ++k) {
+            const int slot = (first + k) % d.incr_cap;
+            if (recs[slot].istep != first + k + 1)
+                return fail(VOCE_ERR_STATE, "increment record %d missing", first + k + 1);
+            if (graph_ok) {
+                // one prelude, 7 launches per iteration, 7 at the increment end
+                r->prof.launches += 1 + 7LL * recs[slot].iters + 7;
+            }
+            collect_increment(r, recs[slot], logs.data() + (size_t)slot * d.iter_max * VOCE_ITLOG);
+        }
+        done += chunk;
     }
     return VOCE_OK;
 }
@@ -807,6 +898,13 @@ int voce_rve_run_timed(voce_rve *r, int n, double *device_ms)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int voce_rve_set_graph(voce_rve *r, int on)
+{
+    if (!r) return fail(VOCE_ERR_ARG, "null argument");
+    r->use_graph = on != 0;
+    return VOCE_OK;
 }
 
 int voce_rve_set_profiling(voce_rve *r, int on)

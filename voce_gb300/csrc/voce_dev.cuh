@@ -85,6 +85,7 @@ struct RveDesc {
     FftPlan1 plx, ply, plz;
     // fields
     double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
+    float *sch32;        // float copy of sch (mixed-precision Newton only)
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl;
     int *phase;
     void *spec, *aacc;
@@ -129,10 +130,12 @@ __host__ __device__ __forceinline__ int sym6(int i, int j)
     return a * 6 - (a * (a - 1)) / 2 + (b - a);
 }
 
-// Newton-Raphson reciprocal: a single-precision seed refined by three steps
-// of r <- r + r(1 - x r) (each step squares the relative error:
-// 2^-23 -> 2^-46 -> 2^-92), falling back to division outside the range
-// where the float seed is meaningful.
+// Newton-Raphson reciprocal: a single-precision seed refined by two steps
+// of r <- r + r(1 - x r), each of which squares the relative error
+// (2^-23 -> 2^-46 -> below 2^-52 up to rounding); outside the range where
+// the float seed is meaningful it falls back to division.  It is used only
+// inside the 6x6 solve of the Newton step, whose accuracy shapes the step
+// and not the converged stress.
 __device__ __forceinline__ double rcp_nr(double x)
 {
     double ax = fabs(x);
@@ -142,9 +145,44 @@ __device__ __forceinline__ double rcp_nr(double x)
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
     r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
     return r;
+}
+
+// single-precision LDL^T solve of the same system (mixed-precision Newton)
+__device__ __forceinline__ void ldlt_solve6f(const float (&M)[6][6], float (&b)[6])
+{
+    float L[6][6], w[6][6], dinv[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        float dj = M[j][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) dj = fmaf(-L[j][k], w[j][k], dj);
+        dinv[j] = 1.0f / dj;
+#pragma unroll
+        for (int i = j + 1; i < 6; ++i) {
+            float sv = M[i][j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) sv = fmaf(-L[i][k], w[j][k], sv);
+            w[i][j] = sv;
+            L[i][j] = sv * dinv[j];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float sv = b[i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) sv = fmaf(-L[i][k], b[k], sv);
+        b[i] = sv;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) b[i] *= dinv[i];
+#pragma unroll
+    for (int i = 5; i >= 0; --i) {
+        float sv = b[i];
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) sv = fmaf(-L[k][i], b[k], sv);
+        b[i] = sv;
+    }
 }
 
 // |r|^e by binary powering (e >= 0), exact integer exponent
@@ -159,48 +197,71 @@ __device__ __forceinline__ double ipow_abs(double a, int e)
     return res;
 }
 
+// |r|^e with a fixed multiplication chain for e = 19 (n = 20): 6 products
+__device__ __forceinline__ double pow_abs_e(double a, int e)
+{
+    if (e == 19) {
+        const double a2 = a * a, a4 = a2 * a2, a8 = a4 * a4, a16 = a8 * a8;
+        return (a16 * a2) * a;
+    }
+    return ipow_abs(a, e);
+}
+
 // ---------------------------------------------------------------------------
 // Flow rule: StrainRate_eval (constitutive.c:126-194) on a stress 5-vector.
 // edot[5] = sum_k sch_k * gdot_k; D (packed 15, 5x5 sym) = sum_k rss1_k sch_k sch_k^T
 // xkin is always zero in the reference (init.c:793) and is left out.
 // ---------------------------------------------------------------------------
-template <bool WANT_D, bool WANT_SYS>
+template <bool WANT_D, bool WANT_SYS, typename DT = double>
 __device__ __forceinline__ void flow_rule(const RveDesc &d, long long v, const double *s,
-                                          double *edot, double *D, double *gd, double *tx)
+                                          double *edot, DT *D, double *gd, double *tx)
 {
     const long long nv = d.nv;
 #pragma unroll
     for (int i = 0; i < 5; ++i) edot[i] = 0.0;
     if (WANT_D) {
 #pragma unroll
-        for (int i = 0; i < 15; ++i) D[i] = 0.0;
+        for (int i = 0; i < 15; ++i) D[i] = DT(0);
     }
     for (int k = 0; k < d.nsys; ++k) {
         double sc[5];
 #pragma unroll
         for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
-        double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
-        int neg = rss < 0.0;
-        double it = __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
-        double r = rss * it;
-        double ap;
-        if (d.ipow_n >= 1) ap = ipow_abs(fabs(r), d.ipow_n - 1);
-        else ap = fabs(pow(r, d.nrs[k] - 1.0));
-        double g1 = d.g0n[k] * ap * it;                      // rss1 = gam0 n |r^(n-1)| / tau
-        double an = (d.ipow_n >= 1) ? ap * fabs(r) : fabs(pow(r, d.nrs[k]));
-        double g2 = d.gam0[k] * an * (r > 0.0 ? 1.0 : -1.0);  // rss2 = gam0 |r^n| sign(r)
+        const double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const int neg = rss < 0.0;
+        const double it = __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
+        const double r = rss * it;
+        double g1, g2;
+        if (d.ipow_n >= 1) {
+            // |r|^(n-1) and |r|^n sign(r) = q r with q = gam0 |r|^(n-1)
+            const double q = d.gam0[k] * pow_abs_e(fabs(r), d.ipow_n - 1);
+            g2 = q * r;                      // rss2 = gam0 |r^n| sign(r)
+            g1 = (q * it) * d.nrs[k];        // rss1 = gam0 n |r^(n-1)| / tau
+        } else {
+            g1 = d.g0n[k] * fabs(pow(r, d.nrs[k] - 1.0)) * it;
+            g2 = d.gam0[k] * fabs(pow(r, d.nrs[k])) * (r > 0.0 ? 1.0 : -1.0);
+        }
         if (WANT_SYS) { gd[k] = g2; tx[k] = g1; }
 #pragma unroll
         for (int i = 0; i < 5; ++i) edot[i] = fma(sc[i], g2, edot[i]);
         if (WANT_D) {
-            double t[5];
+            DT scd[5], t[5];
+            if (sizeof(DT) == 4) {
+                // the single-precision Jacobian reads the float copy of the Schmid vectors
 #pragma unroll
-            for (int i = 0; i < 5; ++i) t[i] = g1 * sc[i];
+                for (int i = 0; i < 5; ++i) scd[i] = (DT)__ldg(d.sch32 + (long long)(5 * k + i) * nv + v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 5; ++i) scd[i] = (DT)sc[i];
+            }
+            const DT gg = (DT)g1;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = gg * scd[i];
             int q = 0;
 #pragma unroll
             for (int i = 0; i < 5; ++i)
 #pragma unroll
-                for (int j = i; j < 5; ++j) { D[q] = fma(t[i], sc[j], D[q]); ++q; }
+                for (int j = i; j < 5; ++j) { D[q] = fma(t[i], scd[j], D[q]); ++q; }
         }
     }
 }

@@ -119,6 +119,7 @@ __device__ void schmid_from_tm(const RveDesc &d, const SetupConst &sc, long long
             double acc = 0.0;
             for (int c = 0; c < 5; ++c) acc += Mr[i][c] * sc.schxt[5 * s + c];
             d.sch[(long long)(5 * s + i) * d.nv + v] = acc;
+            if (d.sch32) d.sch32[(long long)(5 * s + i) * d.nv + v] = (float)acc;
         }
 }
 
@@ -156,6 +157,8 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             for (int c = 0; c < 9; ++c) d.tm[c * nv + v] = (c % 4 == 0) ? 1.0 : 0.0;
             for (int c = 0; c < 21; ++c) d.sg[c * nv + v] = 0.0;
             for (int c = 0; c < 60; ++c) d.sch[c * nv + v] = 0.0;
+            if (d.sch32)
+                for (int c = 0; c < 60; ++c) d.sch32[c * nv + v] = 0.0f;
             for (int c = 0; c < 24; ++c) { d.crss[c * nv + v] = 0.0; d.itau[c * nv + v] = 0.0; }
             continue;
         }
@@ -438,7 +441,11 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int n
 // solved in the equivalent symmetric form
 //   (S0 + S_g + dt dEdot) dsig = S0 R
 // where R is the reference's residual (evolution.c:78-83) and S0 = C0^-1.
+// MIXED_NR: the residual, the update and the stop test stay in FP64; the
+// Jacobian and its LDL^T solve run in FP32 (an inexact Newton step that
+// converges to the same FP64 fixed point).
 // ---------------------------------------------------------------------------
+template <bool MIXED_NR>
 __global__ void __launch_bounds__(128) k_nr(RveDesc d)
 {
     double acc[VOCE_NPART];
@@ -477,10 +484,16 @@ __global__ void __launch_bounds__(128) k_nr(RveDesc d)
         for (int i = 0; i < 6; ++i)
 #pragma unroll
             for (int j = i; j < 6; ++j) P[sym6(i, j)] += d.S0[i * 6 + j];
+        float Pf[21];
+        if (MIXED_NR) {
+#pragma unroll
+            for (int q = 0; q < 21; ++q) Pf[q] = (float)P[q];
+        }
         double sn2 = 0.0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) sn2 = fma(lam[c], lam[c], sn2);
-        const double signorm = sqrt(sn2);
+        // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
+        const double thr = 1e-14 * sn2;
         double sig[6], sp[6], Rl[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) { sig[c] = lam[c]; sp[c] = lam[c]; Rl[c] = 0.0; }
@@ -488,32 +501,57 @@ __global__ void __launch_bounds__(128) k_nr(RveDesc d)
         bool go = true;
         while (go && it < 100) {
             ++it;
-            double ed[5], D[15];
+            double ed[5];
 #pragma unroll
             for (int c = 0; c < 6; ++c) sp[c] = sig[c];
-            flow_rule<true, false>(d, v, sig, ed, D, nullptr, nullptr);
             double R[6];
+            if (MIXED_NR) {
+                float D[15];
+                flow_rule<true, false, float>(d, v, sig, ed, D, nullptr, nullptr);
+                float M[6][6], x[6];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+                for (int i = 0; i < 6; ++i) {
+                    double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
 #pragma unroll
-                for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
-                R[i] = s;
-                Rl[i] = s;
-            }
-            double M[6][6];
-#pragma unroll
-            for (int i = 0; i < 6; ++i)
-#pragma unroll
-                for (int j = 0; j <= i; ++j) {
-                    double m = P[sym6(i, j)];
-                    if (i < 5 && j < 5) {
-                        const int a = j, b = i;  // a <= b
-                        m = fma(dt, D[a * 5 - (a * (a - 1)) / 2 + (b - a)], m);
-                    }
-                    M[i][j] = m;
+                    for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+                    R[i] = s;
+                    Rl[i] = s;
+                    x[i] = (float)s;
                 }
-            ldlt_solve6(M, R);
+                const float dtf = (float)dt;
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+#pragma unroll
+                    for (int j = 0; j <= i; ++j) {
+                        float m = Pf[sym6(i, j)];
+                        if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                        M[i][j] = m;
+                    }
+                ldlt_solve6f(M, x);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
+            } else {
+                double D[15];
+                flow_rule<true, false, double>(d, v, sig, ed, D, nullptr, nullptr);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) {
+                    double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+                    R[i] = s;
+                    Rl[i] = s;
+                }
+                double M[6][6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+#pragma unroll
+                    for (int j = 0; j <= i; ++j) {
+                        double m = P[sym6(i, j)];
+                        if (i < 5 && j < 5) m = fma(dt, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                        M[i][j] = m;
+                    }
+                ldlt_solve6(M, R);
+            }
             double cnr = 0.0;
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
@@ -522,7 +560,7 @@ __global__ void __launch_bounds__(128) k_nr(RveDesc d)
                 cnr = fma(dd, dd, cnr);
                 sig[c] = sn;
             }
-            go = fabs(sqrt(cnr) / signorm) > 1E-7;
+            go = cnr > thr;
         }
         double cs = 0.0, ce = 0.0;
 #pragma unroll
@@ -587,7 +625,7 @@ __device__ double svm_of(const double *t9)
 
 // one thread: errors, volume averages, mixed-BC macro correction,
 // convergence decision (evolution.c:401-431, get_smacro :170-241)
-__global__ void k_finalize_iter(RveDesc d, int npart)
+__global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle cond, int use_cond)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
@@ -622,7 +660,8 @@ __global__ void k_finalize_iter(RveDesc d, int npart)
     m->Err_s = Err_s;
     const int it = m->iter;
     if (it < d.iter_max) {
-        double *lg = d.itlog + VOCE_ITLOG * it;
+        const int slot = (m->istep - 1) % d.incr_cap;
+        double *lg = d.itlog + ((long long)slot * d.iter_max + it) * VOCE_ITLOG;
         lg[0] = Err_e;
         lg[1] = Err_s;
         lg[2] = m->s_vm;
@@ -641,6 +680,7 @@ __global__ void k_finalize_iter(RveDesc d, int npart)
     m->first_iter = 0;
     const bool more = (m->iter < d.iter_max) && (fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
     m->converged = more ? 0 : 1;
+    if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
     if (!more) {
         // epilogue macro bookkeeping (evolution.c:438-461)
         double act[9], vga[9];
@@ -660,7 +700,11 @@ __global__ void k_finalize_iter(RveDesc d, int npart)
         }
         m->e_vm = vm_strain(act);
         m->d_vm = vm_strain(vga);
-        const double *a = m->dDisGradAvg_acum;
+        // the displacement gradient received every dDisGradAvg of this
+        // increment except the last one, which get_smacro computes after the
+        // final update (evolution.c:391 vs :418): only those enter VelGrad
+        double a[9];
+        for (int q = 0; q < 9; ++q) a[q] = m->dDisGradAvg_acum[q] - m->dDisGradAvg[q];
         m->acum_a[0] = 0.5 * (a[5] - a[7]);
         m->acum_a[1] = 0.5 * (a[2] - a[6]);
         m->acum_a[2] = 0.5 * (a[1] - a[3]);
@@ -769,7 +813,7 @@ __global__ void __launch_bounds__(128) k_incr_end(RveDesc d, SetupConst sc)
         if (d.solid[ph]) {
             double sp[6], gd[VOCE_NS], tx[VOCE_NS];
             for (int c = 0; c < 6; ++c) sp[c] = d.sigp[c * nv + v];
-            flow_rule<false, true>(d, v, sp, ed, nullptr, gd, tx);
+            flow_rule<false, true, double>(d, v, sp, ed, (double *)nullptr, gd, tx);
             for (int k = 0; k < d.nsys; ++k) {
                 d.gamdot[k * nv + v] = gd[k];
                 d.taux[k * nv + v] = tx[k];
@@ -1048,7 +1092,8 @@ cudaError_t set_smem_limits(bool mixed, const Tiles &t, const RveDesc &d)
 }
 
 template <typename R>
-cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf)
+cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf,
+                             cudaGraphConditionalHandle cond, int use_cond)
 {
     pf.begin(K_FFT_Z_FWD, s);
     k_fft_z_fwd<R><<<d.nx * (d.ny / t.zrows), 256, smem_lines<R>(d.nz, 3 * t.zrows), s>>>(d, t.zrows);
@@ -1066,15 +1111,18 @@ cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaSt
     k_fft_z_inv<R><<<d.nx * (d.ny / t.zirows), 256, smem_lines<R>(d.nz, 3 * t.zirows), s>>>(d, d.spec, 6, t.zirows, 0);
     pf.end(K_FFT_Z_INV, s);
     pf.begin(K_NR, s);
-    k_nr<<<npart, 128, 0, s>>>(d);
+    if (d.mixed) k_nr<true><<<npart, 128, 0, s>>>(d);
+    else k_nr<false><<<npart, 128, 0, s>>>(d);
     pf.end(K_NR, s);
     pf.begin(K_FIN_ITER, s);
-    k_finalize_iter<<<1, 256, 0, s>>>(d, npart);
+    k_finalize_iter<<<1, 256, 0, s>>>(d, npart, cond, use_cond);
     pf.end(K_FIN_ITER, s);
     return cudaGetLastError();
 }
-template cudaError_t launch_iteration<double>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &);
-template cudaError_t launch_iteration<float>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &);
+template cudaError_t launch_iteration<double>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &,
+                                             cudaGraphConditionalHandle, int);
+template cudaError_t launch_iteration<float>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &,
+                                            cudaGraphConditionalHandle, int);
 
 template <typename R>
 cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,

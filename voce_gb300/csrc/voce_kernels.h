@@ -52,7 +52,8 @@ struct Prof {
 };
 
 template <typename R>
-cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf);
+cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf,
+                             cudaGraphConditionalHandle cond = 0, int use_cond = 0);
 template <typename R>
 cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,
                                  cudaStream_t s, Prof &pf);
