@@ -42,6 +42,9 @@ def parse():
     p.add_argument("--impl", default="voce", choices=["voce", "reference"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3"],
+                   help="cfg2: the headline line (64^3, FP64); cfg3: 256^3 plane-strain "
+                        "compression, FP64 and mixed side by side with the mixed error")
     return p.parse_args()
 
 
@@ -163,6 +166,16 @@ def profiled_traffic():
     return float(k["dram_bytes_per_launch"]) * (64 ** 3) / float(k["voxels"])
 
 
+def fp64_flops_per_newton_iteration():
+    """FP64 flops (FMA = 2) that k_nr executes per Newton iteration of one
+    voxel, from the committed ncu instruction counts."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    k = json.load(open(p)).get("k_nr", {})
+    return k.get("fp64_flops_per_newton_iteration")
+
+
 def cpu_sample(threads: int, iters: int):
     """The oracle (C restatement of the reference) on a bounded sample of
     the workload: the first increment of the 64^3 case capped at `iters`
@@ -237,32 +250,49 @@ def run_voce(args, rank, world, grp):
     slip = capi.read_slip(os.path.join(d, "mat.sx"))
 
     # ---- device-resident leg: K increments timed with CUDA events --------
+    # Each increment runs as one CUDA graph (device-side conditional loop
+    # over the Green iterations); events on the RVE's stream bracket it.
     r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase, prec)
     r.run(args.warmup)
-    r.set_profiling(True)
-    r.reset_kernel_times()
     launches0 = r.kernel_launches
     grp.barrier()
     step_ms = []
     iters = []
+    nr_iters = 0.0
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for k in range(args.steps):
             r.flush_l2(FLUSH_BYTES)
             launches0 += 1        # the flush kernel is not part of the step
             step_ms.append(r.run_timed(1))
-            iters.append(r.increment(args.warmup + k)["iters"])
+            inc = r.increment(args.warmup + k)
+            iters.append(inc["iters"])
+            nr_iters += inc["nr_iters_total"]
     grp.barrier()
     launches = r.kernel_launches - launches0
-    kt = r.kernel_times()
     tot_ms = sum(step_ms)
     t_max = grp.max(tot_ms)
     vox_iters = grp.sum(float(nv * sum(iters)))
     value = vox_iters / (t_max * 1e-3)
+
+    # ---- per-kernel durations: CUDA events around every launch over the
+    # next few increments (host-driven loop, same kernels, same stream) ----
+    n_prof = min(args.steps, 5)
+    r.set_profiling(True)
+    r.reset_kernel_times()
+    prof_nr_iters = 0.0
+    for k in range(n_prof):
+        r.flush_l2(FLUSH_BYTES)
+        r.run(1)
+        prof_nr_iters += r.increment(args.warmup + args.steps + k)["nr_iters_total"]
+    kt = r.kernel_times()
+    r.set_profiling(False)
     nr_ms, nr_n = kt["nr"]
     nr_avg_s = nr_ms * 1e-3 / max(nr_n, 1)
     peak, peak_kind = measured_peaks()
     achieved = NR_BYTES_PER_VOXEL * nv / nr_avg_s / 1e9
     fp64_peak = lib.voce_measure_fp64_tflops()
+    fpi = fp64_flops_per_newton_iteration()
+    fp64_ach = (fpi * prof_nr_iters / (nr_ms * 1e-3) / 1e12) if fpi else None
     r.close()
 
     # ---- end-to-end leg through the C ABI, host buffers ----------------
@@ -330,7 +360,12 @@ def run_voce(args, rank, world, grp):
                      "kernel": "k_nr", "peak_kind": peak_kind,
                      "algorithmic_bytes_per_voxel": NR_BYTES_PER_VOXEL,
                      "avg_launch_ms": nr_avg_s * 1e3},
-        "fp64": {"measured_peak_tflops": fp64_peak},
+        "fp64_roof": {"bound": "fp64", "kernel": "k_nr", "achieved": fp64_ach,
+                      "peak": fp64_peak, "unit": "TFLOP/s",
+                      "frac": (fp64_ach / fp64_peak) if fp64_ach else None,
+                      "peak_kind": "measured by voce_measure_fp64_tflops in this run"},
+        "kernel_timing": "CUDA events around every launch over %d increments after the "
+                         "timed ones (host-driven loop)" % n_prof,
         "kernel_ms": {k: v[0] for k, v in kt.items()},
         "kernel_launches_timed": {k: v[1] for k, v in kt.items()},
         "gpu_launches": launches,
@@ -341,9 +376,65 @@ def run_voce(args, rank, world, grp):
     print(json.dumps(out), flush=True)
 
 
+def run_cfg3(args):
+    """256^3 periodic Voronoi (4096 grains), plane-strain compression: the
+    same increments in FP64 and in the mixed form; the mixed form's error
+    against FP64 on the macro stress curve and on the fields."""
+    import numpy as np
+    from voce_gb300 import capi, synth
+    t0 = time.perf_counter()
+    case = synth.config3(n_steps=250)
+    t_mesh = time.perf_counter() - t0
+    d = tempfile.mkdtemp(prefix="cfg3_")
+    synth.write_sx(os.path.join(d, "mat.sx"), case.mat)
+    synth.write_namelist(os.path.join(d, "input"), case.mesh.dims, case.mat, case.load,
+                         time_step=case.time_step, n_steps=case.n_steps)
+    nl = capi.read_namelist(os.path.join(d, "input"))
+    slip = capi.read_slip(os.path.join(d, "mat.sx"))
+    nv = case.mesh.nvox
+    out = {}
+    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+        r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase, prec)
+        r.run(args.warmup)
+        ms, its = 0.0, 0
+        for k in range(args.steps):
+            r.flush_l2(FLUSH_BYTES)
+            ms += r.run_timed(1)
+            its += r.increment(args.warmup + k)["iters"]
+        incs = [r.increment(k) for k in range(args.warmup + args.steps)]
+        out[name] = {"value": nv * its / (ms * 1e-3), "ms": ms, "iters": its,
+                     "incs": incs, "sig": r.field("sig_voigt"), "edot": r.field("edot_voigt")}
+        r.close()
+    a, b = out["mixed"], out["fp64"]
+    def rel(x, y):
+        x = np.asarray(x, float); y = np.asarray(y, float)
+        return float(np.abs(x - y).max() / np.abs(y).max())
+    macro = max(rel(x["sig_avg"], y["sig_avg"]) for x, y in zip(a["incs"], b["incs"]))
+    res = {
+        "metric": "voxel_iterations_per_s", "value": a["value"], "unit": "voxel-iter/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": a["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32fft", "data": "synthetic",
+        "config": {"workload": "256^3 periodic Voronoi, 4096 grains, Cu FCC, plane-strain "
+                               "compression Lzz=-1e-3/s Lxx=+1e-3/s, 2e-4 per increment "
+                               "(config 3), mixed precision", "voxels": nv,
+                   "mesh_generation_s": t_mesh},
+        "fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"]},
+        "mixed_over_fp64": a["value"] / b["value"],
+        "mixed_error_vs_fp64": {"macro_stress_max_rel": macro,
+                                "sigma_field_max_rel": rel(a["sig"], b["sig"]),
+                                "edot_field_max_rel": rel(a["edot"], b["edot"]),
+                                "iterations_mixed_vs_fp64": [a["iters"], b["iters"]]},
+    }
+    print(json.dumps(res), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.config == "cfg3" and args.impl == "voce":
+        run_cfg3(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
