@@ -42,7 +42,13 @@ def parse():
     p.add_argument("--impl", default="voce", choices=["voce", "reference"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3"],
+    p.add_argument("--rves", type=int, default=512, help="cfg4: RVEs in the batch")
+    p.add_argument("--ticks", type=int, default=120, help="cfg4: timed batch ticks")
+    p.add_argument("--requests", type=int, default=32, help="cfg5: requests in the sample")
+    p.add_argument("--rate", type=float, default=2.0, help="cfg5: Poisson arrival rate, req/s")
+    p.add_argument("--inc-scale", type=float, default=0.1,
+                   help="cfg5: increments per request = round(scale x U{10..80})")
+    p.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
                    help="cfg2: the headline line (64^3, FP64); cfg3: 256^3 plane-strain "
                         "compression, FP64 and mixed side by side with the mixed error")
     return p.parse_args()
@@ -168,12 +174,15 @@ def profiled_traffic():
 
 def fp64_flops_per_newton_iteration():
     """FP64 flops (FMA = 2) that k_nr executes per Newton iteration of one
-    voxel, from the committed ncu instruction counts."""
+    voxel and per voxel per launch, from the committed ncu instruction
+    counts (plain FP64 kernel)."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
         return None
     k = json.load(open(p)).get("k_nr", {})
-    return k.get("fp64_flops_per_newton_iteration")
+    if "fp64_flops_per_newton_iteration" not in k:
+        return None
+    return k["fp64_flops_per_newton_iteration"], k.get("fp64_flops_per_voxel_launch", 0.0)
 
 
 def cpu_sample(threads: int, iters: int):
@@ -291,8 +300,8 @@ def run_voce(args, rank, world, grp):
     peak, peak_kind = measured_peaks()
     achieved = NR_BYTES_PER_VOXEL * nv / nr_avg_s / 1e9
     fp64_peak = lib.voce_measure_fp64_tflops()
-    fpi = fp64_flops_per_newton_iteration()
-    fp64_ach = (fpi * prof_nr_iters / (nr_ms * 1e-3) / 1e12) if fpi else None
+    fpi = fp64_flops_per_newton_iteration() if prec == capi.PREC_FP64 else None
+    fp64_ach = ((fpi[0] * prof_nr_iters + fpi[1] * nv * nr_n) / (nr_ms * 1e-3) / 1e12) if fpi else None
     r.close()
 
     # ---- end-to-end leg through the C ABI, host buffers ----------------
@@ -429,11 +438,208 @@ def run_cfg3(args):
     print(json.dumps(res), flush=True)
 
 
+def _loguniform_int(rng, lo, hi):
+    import math
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def _rve_inputs(case, d, tag):
+    """namelist + .sx for a case (the mesh stays in memory)."""
+    from voce_gb300 import capi, synth
+    sx = os.path.join(d, "mat.sx")
+    if not os.path.exists(sx):
+        synth.write_sx(sx, case.mat)
+    nlp = os.path.join(d, "input_%s" % tag)
+    synth.write_namelist(nlp, case.mesh.dims, case.mat, case.load, time_step=case.time_step,
+                         n_steps=case.n_steps, err=case.err, iter_max=case.iter_max)
+    return capi.read_namelist(nlp), capi.read_slip(sx)
+
+
+def _plain_class_throughput(cases_by_edge, d):
+    """Plain FP64, one RVE at a time (graph mode): voxel-iter/s per grid edge,
+    measured on one increment of one RVE of that edge."""
+    from voce_gb300 import capi
+    thr = {}
+    for edge, case in sorted(cases_by_edge.items()):
+        nl, sx = _rve_inputs(case, d, "plain%d" % edge)
+        r = capi.Rve.create(nl, sx, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase)
+        r.run(1)                                  # warm-up increment (graph build)
+        ms = r.run_timed(1)
+        its = r.increment(1)["iters"]
+        thr[edge] = case.mesh.nvox * its / (ms * 1e-3)
+        r.close()
+    return thr
+
+
+def run_cfg4(args):
+    """Batched form: RVEs with edges drawn from {16,32,48,64}, grains
+    log-uniform 8-512, random traceless loads, 2.5e-4 per increment, FP32
+    FFT + FP64 flow rule, advanced in one batch (one launch per phase per
+    tick, tick loop as a CUDA graph).  Bounded sample: `--ticks` ticks."""
+    import numpy as np
+    from voce_gb300 import capi, synth
+    rng = np.random.Generator(np.random.PCG64(4))
+    d = tempfile.mkdtemp(prefix="cfg4_")
+    t0 = time.perf_counter()
+    cases = []
+    for i in range(args.rves):
+        edge = int(rng.choice([16, 32, 48, 64]))
+        grains = _loguniform_int(rng, 8, 512)
+        load = synth.random_traceless_load(rng)
+        mesh = synth.voronoi_mesh(edge, grains, 10000 + i)
+        cases.append(synth.Case("b%d" % i, mesh, synth.CU_LIKE, load, 0.25, 40))
+    t_gen = time.perf_counter() - t0
+    nv_tot = sum(c.mesh.nvox for c in cases)
+    t0 = time.perf_counter()
+    rves = []
+    for i, c in enumerate(cases):
+        nl, sx = _rve_inputs(c, d, str(i))
+        rves.append(capi.Rve.create(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase,
+                                    capi.PREC_MIXED))
+    t_setup = time.perf_counter() - t0
+    b = capi.Batch(capi.PREC_MIXED)
+    for r in rves:
+        b.add(r, 40)
+    b.run(max_ticks=3)                            # warm-up (graph build)
+    chunk = 20
+    done = 0
+    t0 = time.perf_counter()
+    while done < args.ticks:
+        left = b.run(max_ticks=min(chunk, args.ticks - done))
+        done += min(chunk, args.ticks - done)
+    t_run = time.perf_counter() - t0
+    value = nv_tot * args.ticks / t_run           # every RVE is active every tick (checked)
+    assert left == len(rves), left
+    # accuracy: first increment of a few RVEs against the plain FP64 path alone
+    errs = []
+    for i in range(min(8, len(rves))):
+        if rves[i].increments_done < 1:
+            continue
+        c = cases[i]
+        nl, sx = _rve_inputs(c, d, "ref%d" % i)
+        with capi.Rve.create(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase) as rr:
+            rr.run(1)
+            a = np.array(rves[i].increment(0)["sig_avg"])
+            bb = np.array(rr.increment(0)["sig_avg"])
+            errs.append(float(np.abs(a - bb).max() / np.abs(bb).max()))
+    b.close()
+    for r in rves:
+        r.close()
+    by_edge = {}
+    for c in cases:
+        by_edge.setdefault(c.mesh.dims[0], c)
+    thr = _plain_class_throughput(by_edge, d)
+    t_plain = sum(c.mesh.nvox / thr[c.mesh.dims[0]] for c in cases)   # per iteration of all RVEs
+    plain = nv_tot / t_plain
+    res = {
+        "metric": "voxel_iterations_per_s", "value": value, "unit": "voxel-iter/s", "n_gpus": 1,
+        "steps": args.ticks, "warmup": 3, "ms_per_step": 1e3 * t_run / args.ticks,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32fft",
+        "data": "synthetic",
+        "config": {"workload": "batched: %d RVEs, edges U{16,32,48,64}, grains log-U[8,512], "
+                               "random traceless loads 1e-3/s, 2.5e-4 per increment (config 4), "
+                               "mixed precision, one batch tick per step" % len(cases),
+                   "voxels": nv_tot, "mesh_generation_s": t_gen, "setup_s": t_setup},
+        "plain_fp64_one_at_a_time": {"value": plain, "per_edge": thr},
+        "batched_over_plain": value / plain,
+        "first_increment_macro_err_vs_plain_fp64": errs,
+    }
+    print(json.dumps(res), flush=True)
+
+
+def run_cfg5(args):
+    """Serving form: Poisson arrivals of RVE solve requests (edges
+    U{16,32,64,128}, grains log-U[8,2048], random traceless loads), served
+    with continuous batching (mixed precision), against a plain-FP64 server
+    that solves one request at a time, on the same arrival trace."""
+    import numpy as np
+    from voce_gb300 import capi, synth
+    rng = np.random.Generator(np.random.PCG64(5))
+    d = tempfile.mkdtemp(prefix="cfg5_")
+    reqs = []
+    t_arr = 0.0
+    for i in range(args.requests):
+        t_arr += rng.exponential(1.0 / args.rate)
+        edge = int(rng.choice([16, 32, 64, 128]))
+        grains = _loguniform_int(rng, 8, 2048)
+        load = synth.random_traceless_load(rng)
+        inc = max(1, int(round(args.inc_scale * rng.integers(10, 81))))
+        mesh = synth.voronoi_mesh(edge, min(grains, edge ** 3), 20000 + i)
+        c = synth.Case("q%d" % i, mesh, synth.CU_LIKE, load, 0.2, inc)
+        nl, sx = _rve_inputs(c, d, str(i))
+        reqs.append((t_arr, c, nl, sx, inc))
+
+    def serve(precision, one_at_a_time):
+        budget = 200 << 30
+        lat, vi = [], 0
+        t0 = time.perf_counter()
+        if one_at_a_time:
+            clock = 0.0
+            for (ta, c, nl, sx, inc) in reqs:
+                wait = ta - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+                r = capi.Rve.create(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, precision)
+                r.run(inc)
+                vi += sum(c.mesh.nvox * r.increment(k)["iters"] for k in range(inc))
+                r.field("sig_voigt")
+                r.close()
+                lat.append((time.perf_counter() - t0) - ta)
+            span = time.perf_counter() - t0
+            return lat, vi, span
+        with capi.Server(precision, budget, ticks_per_round=16) as s:
+            ids = []
+            k = 0
+            while True:
+                now = time.perf_counter() - t0
+                while k < len(reqs) and reqs[k][0] <= now:
+                    ta, c, nl, sx, inc = reqs[k]
+                    sub_wall = time.perf_counter() - t0
+                    ids.append((s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, inc),
+                                ta, sub_wall))
+                    k += 1
+                run, que = s.poll()
+                if k == len(reqs) and run == 0 and que == 0:
+                    break
+                if run == 0 and que == 0 and k < len(reqs):
+                    time.sleep(max(0.0, reqs[k][0] - (time.perf_counter() - t0)))
+            span = time.perf_counter() - t0
+            for rid, ta, sub_wall in ids:
+                info = s.info(rid)
+                assert info.status == capi.REQ_DONE, (rid, info.status, info.error)
+                # arrival -> done: time in the server plus the poll delay before submission
+                lat.append((info.t_done - info.t_submit) + (sub_wall - ta))
+                vi += info.voxel_iterations
+        return lat, vi, span
+
+    out = {}
+    for name, prec, single in (("served_mixed", capi.PREC_MIXED, False),
+                               ("plain_fp64_one_at_a_time", capi.PREC_FP64, True)):
+        lat, vi, span = serve(prec, single)
+        out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                     "throughput": vi / span, "makespan_s": span, "voxel_iterations": vi}
+    a, b = out["served_mixed"], out["plain_fp64_one_at_a_time"]
+    res = {
+        "metric": "voxel_iterations_per_s", "value": a["throughput"], "unit": "voxel-iter/s",
+        "n_gpus": 1, "steps": len(reqs), "warmup": 0, "ms_per_step": 1e3 * a["makespan_s"] / len(reqs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32fft",
+        "data": "synthetic",
+        "config": {"workload": "serving: %d Poisson requests at %.2f req/s, edges U{16,32,64,128}, "
+                               "grains log-U[8,2048], random traceless loads, increments "
+                               "round(%.2f x U{10..80}) (config 5 sample), continuous batching, "
+                               "mixed precision" % (len(reqs), args.rate, args.inc_scale)},
+        "served": a, "plain_fp64_one_at_a_time": b,
+        "throughput_ratio": a["throughput"] / b["throughput"],
+        "p50_ratio": b["p50_s"] / a["p50_s"], "p99_ratio": b["p99_s"] / a["p99_s"],
+    }
+    print(json.dumps(res), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
-    if args.config == "cfg3" and args.impl == "voce":
-        run_cfg3(args)
+    if args.impl == "voce" and args.config in ("cfg3", "cfg4", "cfg5"):
+        {"cfg3": run_cfg3, "cfg4": run_cfg4, "cfg5": run_cfg5}[args.config](args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -1,0 +1,48 @@
+/*
+ * voce_batch.h -- batched RVEs: many RVEs of any grid size advanced
+ * together, one kernel launch per phase for the whole batch.
+ *
+ * There is no counterpart in the reference, which runs one RVE per MPI job
+ * (evp.c:7-32).  Every RVE keeps its own state, convergence and increment
+ * count; a batch "tick" advances each RVE that still has work by one
+ * Green-operator iteration (plus its increment end when it converges in
+ * that tick).  Per-RVE sums use the same fixed-order reductions as a lone
+ * RVE, so an RVE gives bit-identical results alone and in any batch.
+ * The tick loop runs on the device as a CUDA graph with a conditional WHILE
+ * node; the host returns when every RVE has done its increments or the
+ * tick budget is spent.
+ */
+#ifndef VOCE_BATCH_H
+#define VOCE_BATCH_H
+
+#include "voce_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct voce_batch voce_batch;
+
+/* All RVEs of a batch have the batch's precision (VOCE_PREC_*). */
+int voce_batch_create(int precision, voce_batch **out);
+/* Schedule n_increments more increments of r (created with
+ * voce_rve_create*) inside the batch.  While it belongs to a batch an RVE is
+ * advanced only by voce_batch_run. */
+int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments);
+/* Take r out (allowed between increments); it keeps its state and can run
+ * alone again. */
+int voce_batch_remove(voce_batch *b, voce_rve *r);
+int voce_batch_size(const voce_batch *b);
+/* Run up to max_ticks ticks; *active_left receives the number of RVEs that
+ * still have increments to do.  Increment records of every RVE are
+ * available afterwards through voce_rve_get_increment. */
+int voce_batch_run(voce_batch *b, int max_ticks, int *active_left);
+/* Ticks run so far. */
+long long voce_batch_ticks(const voce_batch *b);
+/* Detaches the RVEs (they are not destroyed) and frees the batch. */
+int voce_batch_destroy(voce_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,62 @@
+/*
+ * voce_serve.h -- serving RVE solve requests with continuous batching.
+ *
+ * There is no counterpart in the reference (one RVE per MPI job).  A
+ * request is one RVE (namelist, slip data, mesh) and a number of strain
+ * increments, as a multiscale or microstructure-screening caller would send
+ * it.  The server keeps one batch (voce_batch.h) running on the GPU.  Each
+ * voce_server_poll() is one round: admit queued requests first-in first-out
+ * while their device footprint (voce_rve_footprint) fits the HBM budget;
+ * advance the batch by at most ticks_per_round ticks; retire the requests
+ * whose increments are done, which frees their memory for the next
+ * admissions.  Requests that arrive while others run join the running batch
+ * at the next round; fields and hardening state stay on the device between
+ * increments.  Times are seconds on the server's monotonic clock.
+ */
+#ifndef VOCE_SERVE_H
+#define VOCE_SERVE_H
+
+#include "voce_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct voce_server voce_server;
+
+enum { VOCE_REQ_QUEUED = 0, VOCE_REQ_RUNNING = 1, VOCE_REQ_DONE = 2, VOCE_REQ_FAILED = 3 };
+
+typedef struct {
+    long long id;
+    int status;                 /* VOCE_REQ_* */
+    int error;                  /* VOCE_ERR_* when failed */
+    int increments_done, increments_wanted;
+    int dims[3];
+    double t_submit, t_admit, t_done;
+    long long voxel_iterations; /* sum over its increments of voxels x Green iterations */
+    voce_increment last;        /* record of its last increment */
+} voce_request_info;
+
+/* keep_fields: keep the final stress and strain-rate fields (Voigt order,
+ * io.c:321-397) of finished requests on the host. */
+int voce_server_create(int precision, long long hbm_budget_bytes,
+                       int ticks_per_round, int keep_fields, voce_server **out);
+/* Copies the inputs; the request is queued at the current server time. */
+int voce_server_submit(voce_server *s, const voce_namelist *nl,
+                       const voce_slip *slip[2], const voce_mesh *mesh,
+                       int n_increments, long long *id_out);
+/* One round; *running and *queued receive the counts afterwards. */
+int voce_server_poll(voce_server *s, int *running, int *queued);
+double voce_server_now(const voce_server *s);
+int voce_server_info(const voce_server *s, long long id, voce_request_info *out);
+/* Final fields of a finished request kept with keep_fields:
+ * which = 20 (stress) or 21 (plastic strain rate), 6 x nvox doubles. */
+int voce_server_result(const voce_server *s, long long id, int which, double *host_out);
+/* Bytes of device memory the admitted requests hold. */
+long long voce_server_bytes_in_use(const voce_server *s);
+int voce_server_destroy(voce_server *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

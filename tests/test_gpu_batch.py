@@ -1,0 +1,88 @@
+"""Batched RVEs (include/voce_batch.h): every RVE gives the same increment
+records and fields alone and inside a batch of RVEs of other sizes, loads
+and increment counts, bit for bit, in both precisions."""
+import tempfile
+
+import numpy as np
+import pytest
+
+from voce_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    rng = np.random.Generator(np.random.PCG64(2024))
+    out = []
+    for i, (n, g, inc) in enumerate([(8, 5, 3), (16, 20, 2), (12, 9, 4), (24, 30, 2), (16, 1, 3), (32, 40, 1)]):
+        load = synth.random_traceless_load(rng) if i % 2 else synth.tension_z()
+        c = synth.small_case(n, g, 300 + i, n_steps=inc, load=load)
+        c.iter_max = 60
+        out.append((c, inc))
+    return out
+
+
+def _make(case, prec):
+    d = tempfile.mkdtemp(prefix="batch_")
+    return capi.Rve.from_files(case.write(d), prec)
+
+
+def _snapshot(r, n):
+    return ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"),
+            r.field("crss"), r.field("tranmat"))
+
+
+def _same(a, b):
+    ia, sa, ea, ca, ta = a
+    ib, sb, eb, cb, tb = b
+    assert [x["iters"] for x in ia] == [x["iters"] for x in ib]
+    for x, y in zip(ia, ib):
+        assert x["sig_avg"] == y["sig_avg"] and x["s_vm"] == y["s_vm"] and x["evmp"] == y["evmp"]
+    for u, v in ((sa, sb), (ea, eb), (ca, cb), (ta, tb)):
+        assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_alone_equals_in_batch(prec, voce_lib):
+    cases = _cases()
+    alone = []
+    for c, n in cases:
+        with _make(c, prec) as r:
+            r.run(n)
+            alone.append(_snapshot(r, n))
+    rves = [_make(c, prec) for c, _ in cases]
+    with capi.Batch(prec) as b:
+        for r, (c, n) in zip(rves, cases):
+            b.add(r, n)
+        left = b.run()
+        assert left == 0
+        assert b.ticks > 0
+    for r, (c, n), ref in zip(rves, cases, alone):
+        _same(_snapshot(r, n), ref)
+        r.close()
+
+
+def test_tick_budget_resume_and_rejoin(voce_lib):
+    """Stopping on a tick budget mid-increment and resuming gives the same
+    result; an RVE leaves the batch between increments and continues alone."""
+    cases = _cases()[:3]
+    ref = []
+    for c, n in cases:
+        with _make(c, capi.PREC_FP64) as r:
+            r.run(n + 1)
+            ref.append(_snapshot(r, n + 1))
+    rves = [_make(c, capi.PREC_FP64) for c, _ in cases]
+    b = capi.Batch(capi.PREC_FP64)
+    for r, (c, n) in zip(rves, cases):
+        b.add(r, n)
+    steps = 0
+    while b.run(max_ticks=7):
+        steps += 1
+    assert steps > 2
+    for r in rves:
+        b.remove(r)
+    b.close()
+    for r, (c, n), rf in zip(rves, cases, ref):
+        r.run(1)                       # one more increment, alone
+        _same(_snapshot(r, n + 1), rf)
+        r.close()

@@ -1,0 +1,64 @@
+"""Serving with continuous batching (include/voce_serve.h): requests that
+arrive while others run join the running batch; admission respects the HBM
+budget; every result equals the same RVE solved alone, bit for bit."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from voce_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(case):
+    d = tempfile.mkdtemp(prefix="serve_")
+    nlp = case.write(d)
+    return nlp, capi.read_namelist(nlp), capi.read_slip(os.path.join(d, "mat.sx"))
+
+
+def test_requests_alone_and_in_the_mix(voce_lib):
+    rng = np.random.Generator(np.random.PCG64(77))
+    cases = []
+    for i, (n, g, inc) in enumerate([(16, 10, 2), (8, 4, 3), (24, 20, 1), (12, 6, 2), (16, 30, 2), (8, 3, 1)]):
+        c = synth.small_case(n, g, 500 + i, n_steps=inc, load=synth.random_traceless_load(rng))
+        c.iter_max = 40
+        cases.append((c, inc))
+    alone = []
+    for c, n in cases:
+        nlp, _, _ = _inputs(c)
+        with capi.Rve.from_files(nlp) as r:
+            r.run(n)
+            alone.append((r.increment(n - 1), r.field("sig_voigt"), r.field("edot_voigt")))
+    budget = 2 * capi.footprint((24, 24, 24))      # forces queueing
+    with capi.Server(capi.PREC_FP64, budget, ticks_per_round=5, keep_fields=True) as s:
+        ids = []
+        for k, (c, n) in enumerate(cases):
+            _, nl, sx = _inputs(c)
+            ids.append(s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, n))
+            if k % 2:                                # arrivals while others run
+                s.poll()
+                assert s.bytes_in_use <= budget
+        for _ in range(100000):
+            run, que = s.poll()
+            assert s.bytes_in_use <= budget
+            if run == 0 and que == 0:
+                break
+        for rid, (c, n), (inc, sig, edot) in zip(ids, cases, alone):
+            info = s.info(rid)
+            assert info.status == capi.REQ_DONE and info.increments_done == n
+            assert info.t_submit <= info.t_admit <= info.t_done
+            assert info.last.iters == inc["iters"] and list(info.last.sig_avg) == inc["sig_avg"]
+            assert np.array_equal(s.result(rid, "sig_voigt", c.mesh.nvox), sig)
+            assert np.array_equal(s.result(rid, "edot_voigt", c.mesh.nvox), edot)
+
+
+def test_request_larger_than_budget_fails(voce_lib):
+    c = synth.small_case(16, 5, 9, n_steps=1)
+    _, nl, sx = _inputs(c)
+    with capi.Server(capi.PREC_FP64, capi.footprint((8, 8, 8)), ticks_per_round=4) as s:
+        rid = s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, 1)
+        s.poll()
+        info = s.info(rid)
+        assert info.status == capi.REQ_FAILED and info.error == 7

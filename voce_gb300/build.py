@@ -23,7 +23,7 @@ LIB = os.path.join(LIBDIR, "libvoce_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-SOURCES = ["voce_kernels.cu", "voce_api.cu"]
+SOURCES = ["voce_kernels.cu", "voce_api.cu", "voce_server.cpp"]
 
 
 def _nvcc() -> str:

@@ -110,6 +110,24 @@ PROTOTYPES = [
     ("voce_host_alloc", C.c_void_p, [C.c_longlong]),
     ("voce_host_free", None, [C.c_void_p]),
     ("voce_measure_fp64_tflops", C.c_double, []),
+    # voce_batch.h
+    ("voce_batch_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    ("voce_batch_add", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("voce_batch_remove", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("voce_batch_size", C.c_int, [C.c_void_p]),
+    ("voce_batch_run", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    ("voce_batch_ticks", C.c_longlong, [C.c_void_p]),
+    ("voce_batch_destroy", C.c_int, [C.c_void_p]),
+    # voce_serve.h
+    ("voce_server_create", C.c_int, [C.c_int, C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    ("voce_server_submit", C.c_int, [C.c_void_p, C.POINTER(VoceNamelist), C.POINTER(C.POINTER(VoceSlip)),
+                                     C.POINTER(VoceMesh), C.c_int, C.POINTER(C.c_longlong)]),
+    ("voce_server_poll", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("voce_server_now", C.c_double, [C.c_void_p]),
+    ("voce_server_info", C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p]),
+    ("voce_server_result", C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_server_bytes_in_use", C.c_longlong, [C.c_void_p]),
+    ("voce_server_destroy", C.c_int, [C.c_void_p]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -301,3 +319,115 @@ class Rve:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Many RVEs advanced together (include/voce_batch.h)."""
+
+    def __init__(self, precision: int = PREC_FP64):
+        h = C.c_void_p()
+        _check(load().voce_batch_create(precision, C.byref(h)))
+        self._h = h
+        self.members = []
+
+    def add(self, rve: Rve, n_increments: int) -> None:
+        _check(load().voce_batch_add(self._h, rve._h, n_increments))
+        self.members.append(rve)
+
+    def remove(self, rve: Rve) -> None:
+        _check(load().voce_batch_remove(self._h, rve._h))
+        self.members.remove(rve)
+
+    def run(self, max_ticks: int = 1 << 30) -> int:
+        left = C.c_int()
+        _check(load().voce_batch_run(self._h, max_ticks, C.byref(left)))
+        return left.value
+
+    @property
+    def ticks(self) -> int:
+        return int(load().voce_batch_ticks(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            load().voce_batch_destroy(self._h)
+            self._h = None
+            self.members = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("error", C.c_int),
+                ("increments_done", C.c_int), ("increments_wanted", C.c_int),
+                ("dims", C.c_int * 3), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("voxel_iterations", C.c_longlong),
+                ("last", VoceIncrement)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class Server:
+    """Continuous-batching request server (include/voce_serve.h)."""
+
+    def __init__(self, precision: int = PREC_FP64, hbm_budget: int = 64 << 30,
+                 ticks_per_round: int = 8, keep_fields: bool = False):
+        h = C.c_void_p()
+        _check(load().voce_server_create(precision, hbm_budget, ticks_per_round,
+                                         int(keep_fields), C.byref(h)))
+        self._h = h
+
+    def submit(self, nl: VoceNamelist, slip: VoceSlip, euler_deg, grain, phase,
+               n_increments: int, solid_phase: int = 0) -> int:
+        eul = np.ascontiguousarray(euler_deg, dtype=np.float64)
+        gr = np.ascontiguousarray(grain, dtype=np.int32)
+        ph = np.ascontiguousarray(phase, dtype=np.int32)
+        mesh = VoceMesh()
+        mesh.dims = (C.c_int * 3)(*nl.CellDim)
+        mesh.euler_deg = _dptr(eul)
+        mesh.grain = _iptr(gr)
+        mesh.phase = _iptr(ph)
+        sp = (C.POINTER(VoceSlip) * 2)()
+        sp[solid_phase] = C.pointer(slip)
+        rid = C.c_longlong()
+        _check(load().voce_server_submit(self._h, C.byref(nl), sp, C.byref(mesh), n_increments,
+                                         C.byref(rid)))
+        return rid.value
+
+    def poll(self):
+        run = C.c_int()
+        que = C.c_int()
+        _check(load().voce_server_poll(self._h, C.byref(run), C.byref(que)))
+        return run.value, que.value
+
+    def now(self) -> float:
+        return load().voce_server_now(self._h)
+
+    def info(self, rid: int) -> RequestInfo:
+        out = RequestInfo()
+        _check(load().voce_server_info(self._h, rid, C.byref(out)))
+        return out
+
+    def result(self, rid: int, which: str, nv: int) -> np.ndarray:
+        out = np.zeros(6 * nv)
+        _check(load().voce_server_result(self._h, rid, FIELD[which], _dptr(out)))
+        return out.reshape(6, nv)
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(load().voce_server_bytes_in_use(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            load().voce_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -2,6 +2,7 @@
 // and the C ABI declared in include/voce_gpu.h.
 #include "voce_gpu.h"
 #include "voce_gpu_diag.h"
+#include "voce_batch.h"
 #include "voce_kernels.h"
 
 #include <cuda_runtime.h>
@@ -187,6 +188,7 @@ struct voce_rve {
     long long flush_n = 0;
     Prof prof;
     bool use_graph = true;
+    struct voce_batch *batch = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int n_done = 0, n_steps = 0;
@@ -479,7 +481,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         d.nrs[s] = nr;
         d.g0n[s] = sx.gamd0 * nr;
         d.tau0[s] = sx.tau0f;
-        sc.tau0b[s] = sx.tau0b;
+        d.tau0b[s] = sx.tau0b;
         d.tau1[s] = tau1;
         d.thet0[s] = thet0;
         d.thet1[s] = sx.thet1;
@@ -492,7 +494,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         double a[3][3];
         for (int p = 0; p < 3; ++p)
             for (int q = 0; q < 3; ++q) a[p][q] = (n[p] * b[q] + n[q] * b[p]) / 2.0;
-        t_to_v(a, sc.schxt + 5 * s, 5);
+        t_to_v(a, d.schxt + 5 * s, 5);
         for (int q = 0; q < 3; ++q) { d.bn[3 * s + q] = n[q]; d.bb[3 * s + q] = b[q]; }
     }
     {
@@ -639,11 +641,15 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     }
     m.istep = 1;
     m.first_iter = 1;
+    m.active = 1;
+    m.target = 0x7fffffff;
     m.Err_e = 2. * d.err_tol;
     m.Err_s = 2. * d.err_tol;
     CUDA_TRY(cudaMemcpyAsync(d.macro, &m, sizeof(m), cudaMemcpyHostToDevice, r->stream));
     if (r->precision) r->tiles.choose<float>(d);
     else r->tiles.choose<double>(d);
+    d.zrows = r->tiles.zrows; d.yxt = r->tiles.yxt; d.xkc = r->tiles.xkc;
+    d.xkc3 = r->tiles.xkc3; d.zirows = r->tiles.zirows; d.zirows3 = r->tiles.zirows3;
     CUDA_TRY(set_smem_limits(r->precision != 0, r->tiles, d));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     *out = r;
@@ -775,11 +781,68 @@ int build_graph(voce_rve *r)
     return VOCE_OK;
 }
 
+// Copy the records and iteration logs of the increments finished since the
+// last read-back from the device rings (capacity incr_cap increments).
+int collect_new(voce_rve *r, bool count_graph_launches)
+{
+    RveDesc &d = r->d;
+    MacroDev m;
+    CUDA_TRY(cudaMemcpyAsync(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    const int completed = m.istep - 1;
+    const int fresh = completed - r->n_done;
+    if (fresh <= 0) return VOCE_OK;
+    if (fresh > d.incr_cap) return fail(VOCE_ERR_STATE, "increment ring overflow (%d > %d)", fresh, d.incr_cap);
+    std::vector<IncrDev> recs(d.incr_cap);
+    std::vector<double> logs((size_t)d.incr_cap * d.iter_max * VOCE_ITLOG);
+    CUDA_TRY(cudaMemcpyAsync(recs.data(), d.incr, sizeof(IncrDev) * recs.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(logs.data(), d.itlog, sizeof(double) * logs.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    CUDA_TRY(cudaGetLastError());
+    const int first = r->n_done;
+    for (int k = 0; k < fresh; ++k) {
+        const int slot = (first + k) % d.incr_cap;
+        if (recs[slot].istep != first + k + 1)
+            return fail(VOCE_ERR_STATE, "increment record %d missing", first + k + 1);
+        // one prelude, 7 launches per iteration, 7 at the increment end
+        if (count_graph_launches) r->prof.launches += 1 + 7LL * recs[slot].iters + 7;
+        collect_increment(r, recs[slot], logs.data() + (size_t)slot * d.iter_max * VOCE_ITLOG);
+    }
+    return VOCE_OK;
+}
+
+// Grow the record rings to hold `cap` increments (drops the cached graph,
+// whose kernel arguments point at the old rings).
+int ensure_ring(voce_rve *r, int cap)
+{
+    RveDesc &d = r->d;
+    if (cap <= d.incr_cap) return VOCE_OK;
+    int rc = collect_new(r, false);
+    if (rc) return rc;
+    double *lg = nullptr;
+    IncrDev *ic = nullptr;
+    if ((rc = dalloc(r, lg, (size_t)cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1)))) return rc;
+    if ((rc = dalloc(r, ic, (size_t)cap))) return rc;
+    // live slots keep their absolute index modulo the capacity
+    std::vector<IncrDev> old(d.incr_cap);
+    CUDA_TRY(cudaMemcpy(old.data(), d.incr, sizeof(IncrDev) * old.size(), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < d.incr_cap; ++k)
+        if (old[k].istep > 0)
+            CUDA_TRY(cudaMemcpy(ic + (old[k].istep - 1) % cap, &old[k], sizeof(IncrDev), cudaMemcpyHostToDevice));
+    d.itlog = lg;
+    d.incr = ic;
+    d.incr_cap = cap;
+    if (r->graph_exec) { cudaGraphExecDestroy(r->graph_exec); r->graph_exec = nullptr; }
+    if (r->graph) { cudaGraphDestroy(r->graph); r->graph = nullptr; }
+    return VOCE_OK;
+}
+
 }  // namespace
 
 int voce_rve_run(voce_rve *r, int n)
 {
     if (!r || n < 0) return fail(VOCE_ERR_ARG, "bad argument");
+    if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch; run the batch or remove it");
     RveDesc &d = r->d;
     const bool graph_ok = r->use_graph && !r->prof.on && d.iter_max > 0 && d.err_tol != 0.0;
     if (graph_ok && !r->graph_exec) {
@@ -789,7 +852,6 @@ int voce_rve_run(voce_rve *r, int n)
     int done = 0;
     while (done < n) {
         const int chunk = std::min(n - done, d.incr_cap);
-        const int first = r->n_done;
         for (int k = 0; k < chunk; ++k) {
             if (graph_ok) {
                 CUDA_TRY(cudaGraphLaunch(r->graph_exec, r->stream));
@@ -798,23 +860,8 @@ int voce_rve_run(voce_rve *r, int n)
                 if (rc) return rc;
             }
         }
-        // records and iteration logs of the chunk (device rings of incr_cap)
-        std::vector<IncrDev> recs(d.incr_cap);
-        std::vector<double> logs((size_t)d.incr_cap * d.iter_max * VOCE_ITLOG);
-        CUDA_TRY(cudaMemcpyAsync(recs.data(), d.incr, sizeof(IncrDev) * recs.size(), cudaMemcpyDeviceToHost, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(logs.data(), d.itlog, sizeof(double) * logs.size(), cudaMemcpyDeviceToHost, r->stream));
-        CUDA_TRY(cudaStreamSynchronize(r->stream));
-        CUDA_TRY(cudaGetLastError());
-        for (int k = 0; k < chunk; ++k) {
-            const int slot = (first + k) % d.incr_cap;
-            if (recs[slot].istep != first + k + 1)
-                return fail(VOCE_ERR_STATE, "increment record %d missing", first + k + 1);
-            if (graph_ok) {
-                // one prelude, 7 launches per iteration, 7 at the increment end
-                r->prof.launches += 1 + 7LL * recs[slot].iters + 7;
-            }
-            collect_increment(r, recs[slot], logs.data() + (size_t)slot * d.iter_max * VOCE_ITLOG);
-        }
+        int rc = collect_new(r, graph_ok);
+        if (rc) return rc;
         done += chunk;
     }
     return VOCE_OK;
@@ -873,6 +920,7 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out)
 
 int voce_rve_destroy(voce_rve *r)
 {
+    if (r && r->batch) voce_batch_remove(r->batch, r);
     delete r;
     return VOCE_OK;
 }
@@ -962,5 +1010,221 @@ void voce_host_free(void *p)
 }
 
 double voce_measure_fp64_tflops(void) { return measure_fp64_tflops(); }
+
+}  // extern "C"
+
+// ===========================================================================
+// batches (voce_batch.h): many RVEs advanced together, one launch per phase
+// ===========================================================================
+struct voce_batch {
+    int precision = 0;
+    std::vector<voce_rve *> rves;
+    cudaStream_t stream = nullptr;
+    RveDesc *d_descs = nullptr;
+    int2 *d_maps = nullptr;
+    int *d_ctl = nullptr;   // ticks, max_ticks, active_out
+    int *h_ctl = nullptr;   // pinned
+    BatchPlan plan;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool dirty = true;
+    long long ticks_total = 0;
+    void drop_graph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    void drop_plan()
+    {
+        drop_graph();
+        if (d_descs) cudaFree(d_descs);
+        if (d_maps) cudaFree(d_maps);
+        d_descs = nullptr;
+        d_maps = nullptr;
+    }
+    ~voce_batch()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        drop_plan();
+        if (d_ctl) cudaFree(d_ctl);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int set_macro_flags(voce_rve *r, int active, int target, int pending)
+{
+    int v[3] = {active, pending, target};
+    MacroDev *m = r->d.macro;
+    CUDA_TRY(cudaMemcpyAsync(&m->active, &v[0], sizeof(int), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(&m->pending_prelude, &v[1], sizeof(int), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(&m->target, &v[2], sizeof(int), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return VOCE_OK;
+}
+
+// descriptor array + per-phase work lists + the tick graph
+int build_batch(voce_batch *b)
+{
+    b->drop_plan();
+    const int n = (int)b->rves.size();
+    BatchPlan &p = b->plan;
+    p = BatchPlan();
+    p.nrve = n;
+    p.mixed = b->precision != 0;
+    if (n == 0) { b->dirty = false; return VOCE_OK; }
+    std::vector<RveDesc> descs(n);
+    std::vector<std::vector<int2>> maps(BP_COUNT);
+    for (int i = 0; i < n; ++i) {
+        descs[i] = b->rves[i]->d;
+        int u[BP_COUNT];
+        batch_units(descs[i], u);
+        for (int ph = 0; ph < BP_COUNT; ++ph) {
+            for (int k = 0; k < u[ph]; ++k) maps[ph].push_back(make_int2(i, k));
+            p.smem[ph] = std::max(p.smem[ph], batch_smem(descs[i], ph));
+        }
+    }
+    size_t tot = 0;
+    for (int ph = 0; ph < BP_COUNT; ++ph) tot += maps[ph].size();
+    CUDA_TRY(cudaMalloc(&b->d_descs, sizeof(RveDesc) * n));
+    CUDA_TRY(cudaMalloc(&b->d_maps, sizeof(int2) * tot));
+    CUDA_TRY(cudaMemcpy(b->d_descs, descs.data(), sizeof(RveDesc) * n, cudaMemcpyHostToDevice));
+    size_t off = 0;
+    for (int ph = 0; ph < BP_COUNT; ++ph) {
+        CUDA_TRY(cudaMemcpy(b->d_maps + off, maps[ph].data(), sizeof(int2) * maps[ph].size(), cudaMemcpyHostToDevice));
+        p.map[ph] = b->d_maps + off;
+        p.total[ph] = (int)maps[ph].size();
+        off += maps[ph].size();
+    }
+    p.descs = b->d_descs;
+    p.ticks = b->d_ctl;
+    p.max_ticks = b->d_ctl + 1;
+    p.active_out = b->d_ctl + 2;
+    CUDA_TRY(set_batch_smem(p));
+    // graph: WHILE (any RVE active and ticks < max) { tick }
+    cudaGraph_t g;
+    CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond;
+    CUDA_TRY(cudaGraphAddNode(&cond, g, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CUDA_TRY(cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_batch_tick(p, b->stream, h);
+    CUDA_TRY(cudaStreamEndCapture(b->stream, &body));
+    CUDA_TRY(e);
+    CUDA_TRY(cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph = g;
+    b->dirty = false;
+    return VOCE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int voce_batch_create(int precision, voce_batch **out)
+{
+    if (!out) return fail(VOCE_ERR_ARG, "null argument");
+    voce_batch *b = new voce_batch();
+    b->precision = precision == VOCE_PREC_MIXED ? 1 : 0;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_ctl, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_ctl, 4 * sizeof(int));
+    if (e != cudaSuccess) {
+        delete b;
+        return fail(VOCE_ERR_CUDA, "batch setup: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return VOCE_OK;
+}
+
+int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments)
+{
+    if (!b || !r || n_increments < 1) return fail(VOCE_ERR_ARG, "bad argument");
+    if (r->batch) return fail(VOCE_ERR_STATE, "the RVE already belongs to a batch");
+    if (r->precision != b->precision) return fail(VOCE_ERR_ARG, "precision differs from the batch's");
+    int rc = ensure_ring(r, n_increments + 1);
+    if (rc) return rc;
+    // the RVE is at an increment boundary: its next prelude is pending
+    rc = set_macro_flags(r, 1, r->n_done + n_increments, 1);
+    if (rc) return rc;
+    r->batch = b;
+    b->rves.push_back(r);
+    b->dirty = true;
+    return VOCE_OK;
+}
+
+int voce_batch_remove(voce_batch *b, voce_rve *r)
+{
+    if (!b || !r || r->batch != b) return fail(VOCE_ERR_ARG, "the RVE is not in this batch");
+    MacroDev m;
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaMemcpy(&m, r->d.macro, sizeof(m), cudaMemcpyDeviceToHost));
+    if (m.active && m.iter != 0) return fail(VOCE_ERR_STATE, "the RVE is in the middle of an increment");
+    int rc = collect_new(r, false);
+    if (rc) return rc;
+    rc = set_macro_flags(r, 1, 0x7fffffff, 0);
+    if (rc) return rc;
+    b->rves.erase(std::find(b->rves.begin(), b->rves.end(), r));
+    r->batch = nullptr;
+    b->dirty = true;
+    return VOCE_OK;
+}
+
+int voce_batch_size(const voce_batch *b) { return b ? (int)b->rves.size() : -1; }
+
+int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
+{
+    if (!b || max_ticks < 1) return fail(VOCE_ERR_ARG, "bad argument");
+    for (voce_rve *r : b->rves) CUDA_TRY(cudaStreamSynchronize(r->stream));
+    if (b->dirty) {
+        int rc = build_batch(b);
+        if (rc) return rc;
+    }
+    if (b->rves.empty()) {
+        if (active_left) *active_left = 0;
+        return VOCE_OK;
+    }
+    b->h_ctl[0] = 0;
+    b->h_ctl[1] = max_ticks;
+    b->h_ctl[2] = 0;
+    CUDA_TRY(cudaMemcpyAsync(b->d_ctl, b->h_ctl, 3 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
+    CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    CUDA_TRY(cudaGetLastError());
+    b->ticks_total += b->h_ctl[0];
+    for (voce_rve *r : b->rves) {
+        int rc = collect_new(r, false);
+        if (rc) return rc;
+        // launches of a tick are counted per batch, not per RVE
+    }
+    if (active_left) *active_left = b->h_ctl[2];
+    return VOCE_OK;
+}
+
+long long voce_batch_ticks(const voce_batch *b) { return b ? b->ticks_total : -1; }
+
+int voce_batch_destroy(voce_batch *b)
+{
+    if (!b) return VOCE_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (voce_rve *r : b->rves) {
+        collect_new(r, false);
+        set_macro_flags(r, 1, 0x7fffffff, 0);
+        r->batch = nullptr;
+    }
+    delete b;
+    return VOCE_OK;
+}
 
 }  // extern "C"

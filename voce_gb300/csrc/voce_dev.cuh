@@ -50,6 +50,9 @@ struct MacroDev {
     double acum_a[3];    // antisym(dDisGradAvg_acum): A12, A02, A01
     double rsl, rlc, nr_total;
     int iter, iter_total, istep, converged, nr_max, first_iter, done;
+    int active;          // 1 while increments remain (batched runs)
+    int pending_prelude; // 1 after an increment ended inside a batch tick
+    int target;          // last increment to run (batched runs)
     int pad;
 };
 
@@ -83,6 +86,10 @@ struct RveDesc {
     double ua[3];        // antisym(Udot): A12, A02, A01
     int vflag[6], sflag[6];
     FftPlan1 plx, ply, plz;
+    // FFT tiles (lines per block) and the Newton-kernel work split
+    int zrows, yxt, xkc, xkc3, zirows, zirows3;
+    double schxt[VOCE_NS * 5];  // Schmid 5-vectors in crystal axes
+    double tau0b[VOCE_NS];      // backward CRSS start value
     // fields
     double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
     float *sch32;        // float copy of sch (mixed-precision Newton only)

@@ -10,6 +10,8 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 namespace voce {
 
 // ---------------------------------------------------------------------------
@@ -36,6 +38,7 @@ __device__ void block_partials(double (&acc)[VOCE_NPART], double *out)
         for (int w = 1; w < nw; ++w) s = (q == VOCE_NPART - 1) ? fmax(s, red[w][q]) : s + red[w][q];
         out[q] = s;
     }
+    __syncthreads();
 }
 
 // sum the per-block partials of one kernel in a fixed order (one block)
@@ -108,7 +111,7 @@ __device__ void euler_a(double t1, double ph, double t2, double (&a)[3][3])
     a[2][2] = cph;
 }
 
-__device__ void schmid_from_tm(const RveDesc &d, const SetupConst &sc, long long v, const double (&T)[3][3])
+__device__ void schmid_from_tm(const RveDesc &d, long long v, const double (&T)[3][3])
 {
     double a[3][3], Mr[6][6];
     for (int i = 0; i < 3; ++i)
@@ -117,7 +120,7 @@ __device__ void schmid_from_tm(const RveDesc &d, const SetupConst &sc, long long
     for (int s = 0; s < d.nsys; ++s)
         for (int i = 0; i < 5; ++i) {
             double acc = 0.0;
-            for (int c = 0; c < 5; ++c) acc += Mr[i][c] * sc.schxt[5 * s + c];
+            for (int c = 0; c < 5; ++c) acc += Mr[i][c] * d.schxt[5 * s + c];
             d.sch[(long long)(5 * s + i) * d.nv + v] = acc;
             if (d.sch32) d.sch32[(long long)(5 * s + i) * d.nv + v] = (float)acc;
         }
@@ -200,14 +203,14 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
         }
         for (int k = 0; k < d.nsys; ++k) {
             d.crss[(2 * k) * nv + v] = d.tau0[k];
-            d.crss[(2 * k + 1) * nv + v] = sc.tau0b[k];
+            d.crss[(2 * k + 1) * nv + v] = d.tau0b[k];
             d.itau[(2 * k) * nv + v] = 1.0 / d.tau0[k];
-            d.itau[(2 * k + 1) * nv + v] = 1.0 / sc.tau0b[k];
+            d.itau[(2 * k + 1) * nv + v] = 1.0 / d.tau0b[k];
         }
         double T[3][3];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) T[i][j] = a[j][i];
-        schmid_from_tm(d, sc, v, T);
+        schmid_from_tm(d, v, T);
     }
     // voxel count and C066 partial sums (37 values) in three passes of 15
     // (the 16th slot of block_partials is a max and stays unused)
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
 // FFT passes
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256) k_fft_z_fwd(RveDesc d, int rows)
+__device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(256) k_fft_z_fwd(RveDesc d, int rows)
     const int NL = 3 * rows, ldl = NL | 1;
     C *bufB = bufA + nz * ldl;
     const int ytiles = ny / rows;
-    const int x = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * rows;
+    const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const long long vb = ((long long)x * ny + y0) * nz;
     for (int idx = threadIdx.x; idx < 6 * rows * nz; idx += blockDim.x) {
         const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
@@ -265,7 +268,10 @@ __global__ void __launch_bounds__(256) k_fft_z_fwd(RveDesc d, int rows)
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_fft_y(RveDesc d, void *specp, int sign, int xt)
+__global__ void __launch_bounds__(256) k_fft_z_fwd(RveDesc d, int rows) { fft_z_fwd_unit<R>(d, rows, blockIdx.x); }
+
+template <typename R>
+__device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int unit)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -274,8 +280,8 @@ __global__ void __launch_bounds__(256) k_fft_y(RveDesc d, void *specp, int sign,
     const int NL = xt, ldl = NL | 1;
     C *bufB = bufA + ny * ldl;
     const int xtiles = nx / xt;
-    const int line = blockIdx.x / xtiles;  // c * nzh + kz
-    const int x0 = (blockIdx.x % xtiles) * xt;
+    const int line = unit / xtiles;  // c * nzh + kz
+    const int x0 = (unit % xtiles) * xt;
     C *spec = (C *)specp;
     const long long base = ((long long)line * nx + x0) * ny;
     for (int idx = threadIdx.x; idx < xt * ny; idx += blockDim.x) {
@@ -291,7 +297,10 @@ __global__ void __launch_bounds__(256) k_fft_y(RveDesc d, void *specp, int sign,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_fft_x_green(RveDesc d, int kc)
+__global__ void __launch_bounds__(256) k_fft_y(RveDesc d, void *specp, int sign, int xt) { fft_y_unit<R>(d, specp, sign, xt, blockIdx.x); }
+
+template <typename R>
+__device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -300,7 +309,7 @@ __global__ void __launch_bounds__(256) k_fft_x_green(RveDesc d, int kc)
     const int NL = 6 * kc, ldl = NL | 1;
     C *bufB = bufA + nx * ldl;
     const int ytiles = ny / kc;
-    const int kz = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * kc;
+    const int kz = unit / ytiles, y0 = (unit % ytiles) * kc;
     C *spec = (C *)d.spec;
     C *aacc = (C *)d.aacc;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
@@ -352,7 +361,10 @@ __global__ void __launch_bounds__(256) k_fft_x_green(RveDesc d, int kc)
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_fft_x(RveDesc d, void *specp, int ncomp, int sign, int kc)
+__global__ void __launch_bounds__(256) k_fft_x_green(RveDesc d, int kc) { fft_x_green_unit<R>(d, kc, blockIdx.x); }
+
+template <typename R>
+__device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, int kc, int unit)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -361,7 +373,7 @@ __global__ void __launch_bounds__(256) k_fft_x(RveDesc d, void *specp, int ncomp
     const int NL = ncomp * kc, ldl = NL | 1;
     C *bufB = bufA + nx * ldl;
     const int ytiles = ny / kc;
-    const int kz = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * kc;
+    const int kz = unit / ytiles, y0 = (unit % ytiles) * kc;
     C *spec = (C *)specp;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
@@ -377,11 +389,14 @@ __global__ void __launch_bounds__(256) k_fft_x(RveDesc d, void *specp, int ncomp
     }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(256) k_fft_x(RveDesc d, void *specp, int ncomp, int sign, int kc) { fft_x_unit<R>(d, specp, ncomp, sign, kc, blockIdx.x); }
+
 // inverse z transform (Hermitian half spectrum -> real); mode 0 adds the
 // result to the symmetric displacement gradient (evolution.c:383-394),
 // mode 1 writes it (scaled by 1/N) to rotl
 template <typename R>
-__global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int ncomp, int rows, int mode)
+__device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int rows, int mode, int unit)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -392,7 +407,7 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int n
     const int NL = np * rows, ldl = NL | 1;
     C *bufB = bufA + nz * ldl;
     const int ytiles = ny / rows;
-    const int x = blockIdx.x / ytiles, y0 = (blockIdx.x % ytiles) * rows;
+    const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const C *spec = (const C *)specp;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long xy = (long long)x * ny + y0;
@@ -436,6 +451,9 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int n
     }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int ncomp, int rows, int mode) { fft_z_inv_unit<R>(d, specp, ncomp, rows, mode, blockIdx.x); }
+
 // ---------------------------------------------------------------------------
 // per-voxel Newton-Raphson stress update (UpdateStress, evolution.c:3-168),
 // solved in the equivalent symmetric form
@@ -446,15 +464,15 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int n
 // converges to the same FP64 fixed point).
 // ---------------------------------------------------------------------------
 template <bool MIXED_NR>
-__global__ void __launch_bounds__(128) k_nr(RveDesc d)
+__device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 {
     double acc[VOCE_NPART];
 #pragma unroll
     for (int q = 0; q < VOCE_NPART; ++q) acc[q] = 0.0;
     const long long nv = d.nv;
     const double dt = d.dt;
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
-         v += (long long)gridDim.x * blockDim.x) {
+    for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
+         v += (long long)nunits * blockDim.x) {
         const int ph = d.phase[v];
         if (!d.solid[ph]) {
 #pragma unroll
@@ -585,8 +603,11 @@ __global__ void __launch_bounds__(128) k_nr(RveDesc d)
         acc[14] += (double)it;
         acc[15] = fmax(acc[15], (double)it);
     }
-    block_partials(acc, d.part + (long long)blockIdx.x * VOCE_NPART);
+    block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
+
+template <bool MIXED_NR>
+__global__ void __launch_bounds__(128) k_nr(RveDesc d) { nr_unit<MIXED_NR>(d, blockIdx.x, gridDim.x); }
 
 __device__ double vm_strain(const double *t)  // VonMises, evolution.c:243-262
 {
@@ -625,7 +646,7 @@ __device__ double svm_of(const double *t9)
 
 // one thread: errors, volume averages, mixed-BC macro correction,
 // convergence decision (evolution.c:401-431, get_smacro :170-241)
-__global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle cond, int use_cond)
+__device__ void finalize_iter_body(const RveDesc &d, int npart, cudaGraphConditionalHandle cond, int use_cond)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
@@ -678,6 +699,7 @@ __global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle
     double t6[6] = {g[0], g[4], g[8], 0.5 * (g[5] + g[7]), 0.5 * (g[2] + g[6]), 0.5 * (g[1] + g[3])};
     t6_to_b<double>(t6, m->ddg6);
     m->first_iter = 0;
+    m->pending_prelude = 0;
     const bool more = (m->iter < d.iter_max) && (fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
     m->converged = more ? 0 : 1;
     if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
@@ -709,6 +731,11 @@ __global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle
         m->acum_a[1] = 0.5 * (a[2] - a[6]);
         m->acum_a[2] = 0.5 * (a[1] - a[3]);
     }
+}
+
+__global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle cond, int use_cond)
+{
+    finalize_iter_body(d, npart, cond, use_cond);
 }
 
 // Harden one voxel: harden() body (constitutive.c:261-305)
@@ -778,7 +805,7 @@ __device__ void orientation(double (&tran)[3][3], double (&rot)[3][3])
 
 // increment epilogue (evolution.c:433-530; update_orient constitutive.c:171-248; harden :250-310;
 // update_schmid kinematics.c:426-459)
-__global__ void __launch_bounds__(128) k_incr_end(RveDesc d, SetupConst sc)
+__device__ void incr_end_unit(const RveDesc &d, int unit, int nunits)
 {
     double acc[VOCE_NPART];
     for (int q = 0; q < VOCE_NPART; ++q) acc[q] = 0.0;
@@ -796,8 +823,8 @@ __global__ void __launch_bounds__(128) k_incr_end(RveDesc d, SetupConst sc)
         dga_start_c[1] = 0.5 * (p[2] - p[6]);
         dga_start_c[2] = 0.5 * (p[1] - p[3]);
     }
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
-         v += (long long)gridDim.x * blockDim.x) {
+    for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
+         v += (long long)nunits * blockDim.x) {
         const int ph = d.phase[v];
         // antisymmetric displacement gradient bookkeeping
         double rl[3];
@@ -886,7 +913,7 @@ __global__ void __launch_bounds__(128) k_incr_end(RveDesc d, SetupConst sc)
                 orientation(T, Rot);
                 for (int a = 0; a < 3; ++a)
                     for (int b = 0; b < 3; ++b) d.tm[(3 * a + b) * nv + v] = T[a][b];
-                schmid_from_tm(d, sc, v, T);
+                schmid_from_tm(d, v, T);
             }
             if (hrd) harden_voxel(d, v, gd);
         } else {
@@ -894,12 +921,14 @@ __global__ void __launch_bounds__(128) k_incr_end(RveDesc d, SetupConst sc)
         }
         for (int c = 0; c < 5; ++c) { acc[c] += e5[c]; acc[6 + c] += ed[c]; }
     }
-    block_partials(acc, d.part + (long long)blockIdx.x * VOCE_NPART);
+    block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
+
+__global__ void __launch_bounds__(128) k_incr_end(RveDesc d) { incr_end_unit(d, blockIdx.x, gridDim.x); }
 
 // increment prelude (evolution.c:306-318): DisGrad += Udot dt, or, under
 // creep, DisGrad := DisGradAvg_actual of the previous increment
-__global__ void k_prelude(RveDesc d)
+__device__ void prelude_unit(const RveDesc &d, int unit, int nunits)
 {
     const MacroDev *m = d.macro;
     double set6[6];
@@ -909,15 +938,17 @@ __global__ void k_prelude(RveDesc d)
         t6_to_b<double>(t6, set6);
     }
     const long long nv = d.nv;
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
-         v += (long long)gridDim.x * blockDim.x)
+    for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
+         v += (long long)nunits * blockDim.x)
         for (int c = 0; c < 6; ++c) {
             if (d.creep) d.dgs[c * nv + v] = set6[c];
             else d.dgs[c * nv + v] += d.u6[c] * d.dt;
         }
 }
 
-__global__ void k_finalize_incr(RveDesc d, int npart)
+__global__ void k_prelude(RveDesc d) { prelude_unit(d, blockIdx.x, gridDim.x); }
+
+__device__ void finalize_incr_body(const RveDesc &d, int npart)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
@@ -961,6 +992,8 @@ __global__ void k_finalize_incr(RveDesc d, int npart)
     }
     // reset for the next increment (evolution.c:330-340)
     m->istep += 1;
+    if (m->istep > m->target) { m->active = 0; m->pending_prelude = 0; }
+    else m->pending_prelude = 1;
     m->iter = 0;
     m->converged = 0;
     m->first_iter = 1;
@@ -972,6 +1005,8 @@ __global__ void k_finalize_incr(RveDesc d, int npart)
     for (int q = 0; q < 6; ++q) m->ddg6[q] = 0.0;
     for (int q = 0; q < 3; ++q) m->acum_a[q] = 0.0;
 }
+
+__global__ void k_finalize_incr(RveDesc d, int npart) { finalize_incr_body(d, npart); }
 
 // fields in the reference's layouts, for download
 __global__ void k_field_out(RveDesc d, int field, double *out)
@@ -1027,6 +1062,150 @@ __global__ void k_field_out(RveDesc d, int field, double *out)
             break;
         default: break;
         }
+    }
+}
+
+
+// ===========================================================================
+// batched entry points: one launch per phase covers many RVEs.  Work item w
+// of a phase is map[w] = (rve, unit); the unit functions are the ones the
+// single-RVE kernels call, so an RVE computes the same numbers alone and in
+// a batch.  RVEs are skipped per phase by their macro flags.
+// ===========================================================================
+enum { MASK_ACTIVE = 0, MASK_CONVERGED = 1, MASK_PRELUDE = 2 };
+
+__device__ __forceinline__ bool unit_on(const RveDesc &d, int mask)
+{
+    const MacroDev *m = d.macro;
+    if (!m->active) return false;
+    if (mask == MASK_CONVERGED) return m->converged != 0;
+    if (mask == MASK_PRELUDE) return m->pending_prelude != 0;
+    return true;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) kb_fft_z_fwd(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_ACTIVE)) continue;
+        fft_z_fwd_unit<R>(d, d.zrows, e.y);
+        __syncthreads();
+    }
+}
+
+// which: 0 spectrum forward, 1 spectrum inverse, 2 antisymmetric accumulator inverse
+template <typename R>
+__global__ void __launch_bounds__(256) kb_fft_y(const RveDesc *descs, const int2 *map, int total, int which)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, which == 2 ? MASK_CONVERGED : MASK_ACTIVE)) continue;
+        fft_y_unit<R>(d, which == 2 ? d.aacc : d.spec, which == 0 ? -1 : +1, d.yxt, e.y);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) kb_fft_x_green(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_ACTIVE)) continue;
+        fft_x_green_unit<R>(d, d.xkc, e.y);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) kb_fft_x_aacc(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_CONVERGED)) continue;
+        fft_x_unit<R>(d, d.aacc, 3, +1, d.xkc3, e.y);
+        __syncthreads();
+    }
+}
+
+// mode 0: spectrum -> displacement gradient; 1: accumulator -> rotl
+template <typename R>
+__global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const int2 *map, int total, int mode)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, mode == 0 ? MASK_ACTIVE : MASK_CONVERGED)) continue;
+        if (mode == 0) fft_z_inv_unit<R>(d, d.spec, 6, d.zirows, 0, e.y);
+        else fft_z_inv_unit<R>(d, d.aacc, 3, d.zirows3, 1, e.y);
+        __syncthreads();
+    }
+}
+
+template <bool MIXED_NR>
+__global__ void __launch_bounds__(128) kb_nr(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_ACTIVE)) continue;
+        nr_unit<MIXED_NR>(d, e.y, d.npart);
+    }
+}
+
+__global__ void __launch_bounds__(128) kb_incr_end(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_CONVERGED)) continue;
+        incr_end_unit(d, e.y, d.npart);
+    }
+}
+
+__global__ void __launch_bounds__(128) kb_prelude(const RveDesc *descs, const int2 *map, int total)
+{
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int2 e = map[w];
+        const RveDesc &d = descs[e.x];
+        if (!unit_on(d, MASK_PRELUDE)) continue;
+        prelude_unit(d, e.y, d.npart);
+    }
+}
+
+// one block per RVE
+__global__ void __launch_bounds__(256) kb_finalize(const RveDesc *descs, int nrve, int incr_end)
+{
+    for (int r = blockIdx.x; r < nrve; r += gridDim.x) {
+        const RveDesc &d = descs[r];
+        if (!unit_on(d, incr_end ? MASK_CONVERGED : MASK_ACTIVE)) continue;
+        if (incr_end) finalize_incr_body(d, d.npart);
+        else finalize_iter_body(d, d.npart, 0, 0);
+        __syncthreads();
+    }
+}
+
+// loop condition of the batch: continue while any RVE is active and the
+// tick budget is not spent
+__global__ void kb_cond(const RveDesc *descs, int nrve, int *ticks, const int *max_ticks,
+                        int *active_out, cudaGraphConditionalHandle cond)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    int a = 0;
+    for (int r = threadIdx.x; r < nrve; r += blockDim.x) a += descs[r].macro->active;
+    if (a) atomicAdd(&any, a);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = *ticks + 1;
+        *ticks = t;
+        *active_out = any;
+        cudaGraphSetConditional(cond, (any > 0 && t < *max_ticks) ? 1u : 0u);
     }
 }
 
@@ -1134,7 +1313,7 @@ cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const T
     k_fft_z_inv<R><<<d.nx * (d.ny / t.zirows3), 256, smem_lines<R>(d.nz, 2 * t.zirows3), s>>>(d, d.aacc, 3, t.zirows3, 1);
     pf.end(K_INC_FFT, s, 3);
     pf.begin(K_INCR_END, s);
-    k_incr_end<<<npart, 128, 0, s>>>(d, sc);
+    k_incr_end<<<npart, 128, 0, s>>>(d);
     pf.end(K_INCR_END, s);
     pf.begin(K_FIN_INCR, s);
     k_finalize_incr<<<1, 256, 0, s>>>(d, npart);
@@ -1145,6 +1324,90 @@ template cudaError_t launch_increment_end<double>(const RveDesc &, const SetupCo
                                                   cudaStream_t, Prof &);
 template cudaError_t launch_increment_end<float>(const RveDesc &, const SetupConst &, const Tiles &, int,
                                                  cudaStream_t, Prof &);
+
+void batch_units(const RveDesc &d, int u[BP_COUNT])
+{
+    u[BP_NP] = d.npart;
+    u[BP_ZF] = d.nx * (d.ny / d.zrows);
+    u[BP_Y6] = 6 * d.nzh * (d.nx / d.yxt);
+    u[BP_XG] = d.nzh * (d.ny / d.xkc);
+    u[BP_ZI] = d.nx * (d.ny / d.zirows);
+    u[BP_X3] = d.nzh * (d.ny / d.xkc3);
+    u[BP_Y3] = 3 * d.nzh * (d.nx / d.yxt);
+    u[BP_Z3] = d.nx * (d.ny / d.zirows3);
+}
+
+template <typename R>
+static size_t batch_smem_t(const RveDesc &d, int ph)
+{
+    switch (ph) {
+    case BP_ZF: return smem_lines<R>(d.nz, 3 * d.zrows);
+    case BP_Y6: case BP_Y3: return smem_lines<R>(d.ny, d.yxt);
+    case BP_XG: return smem_lines<R>(d.nx, 6 * d.xkc);
+    case BP_ZI: return smem_lines<R>(d.nz, 3 * d.zirows);
+    case BP_X3: return smem_lines<R>(d.nx, 3 * d.xkc3);
+    case BP_Z3: return smem_lines<R>(d.nz, 2 * d.zirows3);
+    default: return 0;
+    }
+}
+
+size_t batch_smem(const RveDesc &d, int ph)
+{
+    return d.mixed ? batch_smem_t<float>(d, ph) : batch_smem_t<double>(d, ph);
+}
+
+template <typename R>
+static cudaError_t set_batch_smem_t(const BatchPlan &bp)
+{
+    auto set = [](const void *fn, size_t b) {
+        if (b) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+    };
+    set((const void *)kb_fft_z_fwd<R>, bp.smem[BP_ZF]);
+    set((const void *)kb_fft_y<R>, std::max(bp.smem[BP_Y6], bp.smem[BP_Y3]));
+    set((const void *)kb_fft_x_green<R>, bp.smem[BP_XG]);
+    set((const void *)kb_fft_x_aacc<R>, bp.smem[BP_X3]);
+    set((const void *)kb_fft_z_inv<R>, std::max(bp.smem[BP_ZI], bp.smem[BP_Z3]));
+    return cudaGetLastError();
+}
+
+cudaError_t set_batch_smem(const BatchPlan &bp)
+{
+    return bp.mixed ? set_batch_smem_t<float>(bp) : set_batch_smem_t<double>(bp);
+}
+
+static int grid_for(int total, int cap)
+{
+    return total < cap ? (total > 0 ? total : 1) : cap;
+}
+
+template <typename R>
+static void batch_tick_t(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond)
+{
+    const int FG = 152 * 4, NG = 152 * 2;
+    const RveDesc *D = bp.descs;
+    kb_prelude<<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0);
+    kb_fft_x_green<R><<<grid_for(bp.total[BP_XG], FG), 256, bp.smem[BP_XG], s>>>(D, bp.map[BP_XG], bp.total[BP_XG]);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 1);
+    kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
+    if (bp.mixed) kb_nr<true><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    else kb_nr<false><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 0);
+    kb_fft_x_aacc<R><<<grid_for(bp.total[BP_X3], FG), 256, bp.smem[BP_X3], s>>>(D, bp.map[BP_X3], bp.total[BP_X3]);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y3], FG), 256, bp.smem[BP_Y3], s>>>(D, bp.map[BP_Y3], bp.total[BP_Y3], 2);
+    kb_fft_z_inv<R><<<grid_for(bp.total[BP_Z3], FG), 256, bp.smem[BP_Z3], s>>>(D, bp.map[BP_Z3], bp.total[BP_Z3], 1);
+    kb_incr_end<<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 1);
+    kb_cond<<<1, 256, 0, s>>>(D, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, cond);
+}
+
+cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond)
+{
+    if (bp.mixed) batch_tick_t<float>(bp, s, cond);
+    else batch_tick_t<double>(bp, s, cond);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s)

@@ -9,8 +9,6 @@ struct SetupConst {
     double cxt[36], sxt[36];  // crystal stiffness / compliance, 6-vector basis
     double d6[6];             // B-basis sym(DisGradAvg) at t=0 (init.c:495-499)
     double sc6[6];            // B-basis Scauchy (creep start stress, init.c:523-525)
-    double tau0b[VOCE_NS];    // backward CRSS start value
-    double schxt[VOCE_NS * 5];  // Schmid 5-vectors in crystal axes
 };
 
 // FFT tile sizes (lines per block) for one grid
@@ -58,6 +56,28 @@ template <typename R>
 cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,
                                  cudaStream_t s, Prof &pf);
 cudaError_t set_smem_limits(bool mixed, const Tiles &t, const RveDesc &d);
+
+// Work lists of one batch (device memory): per phase, (rve, unit) pairs.
+enum BatchPhase {
+    BP_NP = 0,   // Newton / increment-end / prelude units (npart per RVE)
+    BP_ZF, BP_Y6, BP_XG, BP_ZI, BP_X3, BP_Y3, BP_Z3, BP_COUNT
+};
+struct BatchPlan {
+    const RveDesc *descs = nullptr;   // device array [nrve]
+    int nrve = 0;
+    const int2 *map[BP_COUNT] = {};
+    int total[BP_COUNT] = {};
+    size_t smem[BP_COUNT] = {};       // dynamic shared memory of the FFT phases
+    int *ticks = nullptr, *max_ticks = nullptr, *active_out = nullptr;
+    bool mixed = false;
+};
+// units of one RVE in each phase
+void batch_units(const RveDesc &d, int units[BP_COUNT]);
+size_t batch_smem(const RveDesc &d, int phase);
+cudaError_t set_batch_smem(const BatchPlan &bp);
+// one tick: prelude (pending), one Green iteration of every active RVE, the
+// increment end of every RVE that converged, the loop condition
+cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond);
 cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
 double measure_fp64_tflops();
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,

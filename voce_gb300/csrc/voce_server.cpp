@@ -1,0 +1,222 @@
+// Continuous-batching request server over the public C ABI (voce_serve.h).
+#include "voce_batch.h"
+#include "voce_gpu.h"
+#include "voce_serve.h"
+
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct Request {
+    voce_request_info info;
+    voce_namelist nl;
+    voce_slip slip[2];
+    bool has_slip[2] = {false, false};
+    std::vector<double> euler;
+    std::vector<int> grain, phase;
+    voce_rve *rve = nullptr;
+    long long footprint = 0;
+    std::vector<double> sig, edot;  // kept fields (Voigt, 6 x nvox)
+};
+
+}  // namespace
+
+struct voce_server {
+    int precision = 0;
+    long long budget = 0, in_use = 0;
+    int ticks_per_round = 1;
+    bool keep_fields = false;
+    voce_batch *batch = nullptr;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    long long next_id = 1;
+    std::map<long long, std::unique_ptr<Request>> reqs;
+    std::deque<long long> queue;
+    std::vector<long long> running;
+    double now() const
+    {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+void retire(voce_server *s, Request &q, int error)
+{
+    if (q.rve) {
+        if (!error) {
+            int n = voce_rve_increments_done(q.rve);
+            q.info.increments_done = n;
+            long long vi = 0;
+            const long long nv = (long long)q.info.dims[0] * q.info.dims[1] * q.info.dims[2];
+            for (int k = 0; k < n; ++k) {
+                voce_increment rec;
+                if (voce_rve_get_increment(q.rve, k, &rec) == VOCE_OK) {
+                    vi += nv * rec.iters;
+                    q.info.last = rec;
+                }
+            }
+            q.info.voxel_iterations = vi;
+            if (s->keep_fields) {
+                q.sig.resize(6 * nv);
+                q.edot.resize(6 * nv);
+                voce_rve_get_field(q.rve, VOCE_FIELD_SIG_VOIGT, q.sig.data());
+                voce_rve_get_field(q.rve, VOCE_FIELD_EDOT_VOIGT, q.edot.data());
+            }
+        }
+        voce_batch_remove(s->batch, q.rve);
+        voce_rve_destroy(q.rve);
+        q.rve = nullptr;
+        s->in_use -= q.footprint;
+    }
+    q.info.status = error ? VOCE_REQ_FAILED : VOCE_REQ_DONE;
+    q.info.error = error;
+    q.info.t_done = s->now();
+    // inputs are no longer needed
+    std::vector<double>().swap(q.euler);
+    std::vector<int>().swap(q.grain);
+    std::vector<int>().swap(q.phase);
+}
+
+}  // namespace
+
+extern "C" {
+
+int voce_server_create(int precision, long long budget, int ticks_per_round, int keep_fields,
+                       voce_server **out)
+{
+    if (!out || budget <= 0 || ticks_per_round < 1) return VOCE_ERR_ARG;
+    voce_server *s = new voce_server();
+    s->precision = precision == VOCE_PREC_MIXED ? VOCE_PREC_MIXED : VOCE_PREC_FP64;
+    s->budget = budget;
+    s->ticks_per_round = ticks_per_round;
+    s->keep_fields = keep_fields != 0;
+    int rc = voce_batch_create(s->precision, &s->batch);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return VOCE_OK;
+}
+
+int voce_server_submit(voce_server *s, const voce_namelist *nl, const voce_slip *slip[2],
+                       const voce_mesh *mesh, int n_increments, long long *id_out)
+{
+    if (!s || !nl || !mesh || !mesh->euler_deg || !mesh->phase || n_increments < 1) return VOCE_ERR_ARG;
+    auto q = std::make_unique<Request>();
+    std::memset(&q->info, 0, sizeof(q->info));
+    q->nl = *nl;
+    for (int p = 0; p < 2; ++p)
+        if (slip && slip[p]) { q->slip[p] = *slip[p]; q->has_slip[p] = true; }
+    const long long nv = (long long)mesh->dims[0] * mesh->dims[1] * mesh->dims[2];
+    q->euler.assign(mesh->euler_deg, mesh->euler_deg + 3 * nv);
+    q->phase.assign(mesh->phase, mesh->phase + nv);
+    if (mesh->grain) q->grain.assign(mesh->grain, mesh->grain + nv);
+    else q->grain.assign(nv, 1);
+    std::memcpy(q->info.dims, mesh->dims, sizeof(q->info.dims));
+    q->info.id = s->next_id++;
+    q->info.status = VOCE_REQ_QUEUED;
+    q->info.increments_wanted = n_increments;
+    q->info.t_submit = s->now();
+    q->footprint = voce_rve_footprint(mesh->dims, s->precision);
+    if (id_out) *id_out = q->info.id;
+    s->queue.push_back(q->info.id);
+    s->reqs[q->info.id] = std::move(q);
+    return VOCE_OK;
+}
+
+int voce_server_poll(voce_server *s, int *running, int *queued)
+{
+    if (!s) return VOCE_ERR_ARG;
+    // admission: first in, first out, while the footprint fits
+    while (!s->queue.empty()) {
+        Request &q = *s->reqs[s->queue.front()];
+        if (q.footprint > s->budget) {
+            s->queue.pop_front();
+            retire(s, q, VOCE_ERR_NOMEM);
+            continue;
+        }
+        if (s->in_use + q.footprint > s->budget) break;
+        s->queue.pop_front();
+        voce_mesh m;
+        std::memcpy(m.dims, q.info.dims, sizeof(m.dims));
+        m.euler_deg = q.euler.data();
+        m.grain = q.grain.data();
+        m.phase = q.phase.data();
+        const voce_slip *sp[2] = {q.has_slip[0] ? &q.slip[0] : nullptr, q.has_slip[1] ? &q.slip[1] : nullptr};
+        int rc = voce_rve_create(&q.nl, sp, &m, s->precision, &q.rve);
+        if (rc == VOCE_OK) rc = voce_batch_add(s->batch, q.rve, q.info.increments_wanted);
+        if (rc != VOCE_OK) {
+            if (q.rve) { voce_rve_destroy(q.rve); q.rve = nullptr; }
+            retire(s, q, rc);
+            continue;
+        }
+        s->in_use += q.footprint;
+        q.info.status = VOCE_REQ_RUNNING;
+        q.info.t_admit = s->now();
+        s->running.push_back(q.info.id);
+    }
+    if (!s->running.empty()) {
+        int left = 0;
+        int rc = voce_batch_run(s->batch, s->ticks_per_round, &left);
+        if (rc) return rc;
+        std::vector<long long> still;
+        for (long long id : s->running) {
+            Request &q = *s->reqs[id];
+            int done = voce_rve_increments_done(q.rve);
+            q.info.increments_done = done;
+            if (done >= q.info.increments_wanted) retire(s, q, 0);
+            else still.push_back(id);
+        }
+        s->running.swap(still);
+    }
+    if (running) *running = (int)s->running.size();
+    if (queued) *queued = (int)s->queue.size();
+    return VOCE_OK;
+}
+
+double voce_server_now(const voce_server *s) { return s ? s->now() : -1.0; }
+
+int voce_server_info(const voce_server *s, long long id, voce_request_info *out)
+{
+    if (!s || !out) return VOCE_ERR_ARG;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return VOCE_ERR_ARG;
+    *out = it->second->info;
+    if (it->second->rve) out->increments_done = voce_rve_increments_done(it->second->rve);
+    return VOCE_OK;
+}
+
+int voce_server_result(const voce_server *s, long long id, int which, double *host_out)
+{
+    if (!s || !host_out) return VOCE_ERR_ARG;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || it->second->info.status != VOCE_REQ_DONE) return VOCE_ERR_STATE;
+    const std::vector<double> &v = which == VOCE_FIELD_EDOT_VOIGT ? it->second->edot : it->second->sig;
+    if (v.empty()) return VOCE_ERR_STATE;
+    std::memcpy(host_out, v.data(), sizeof(double) * v.size());
+    return VOCE_OK;
+}
+
+long long voce_server_bytes_in_use(const voce_server *s) { return s ? s->in_use : -1; }
+
+int voce_server_destroy(voce_server *s)
+{
+    if (!s) return VOCE_OK;
+    for (auto &kv : s->reqs)
+        if (kv.second->rve) {
+            voce_batch_remove(s->batch, kv.second->rve);
+            voce_rve_destroy(kv.second->rve);
+        }
+    voce_batch_destroy(s->batch);
+    delete s;
+    return VOCE_OK;
+}
+
+}  // extern "C"
