@@ -189,6 +189,11 @@ struct voce_rve {
     Prof prof;
     bool use_graph = true;
     struct voce_batch *batch = nullptr;
+    // a lone RVE runs as a plan of one, with the same kernels as a batch
+    BatchPlan plan;
+    RveDesc *plan_desc = nullptr;
+    int2 *plan_maps = nullptr;
+    bool plan_dirty = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int n_done = 0, n_steps = 0;
@@ -199,6 +204,8 @@ struct voce_rve {
         if (stream) cudaStreamSynchronize(stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
+        if (plan_desc) cudaFree(plan_desc);
+        if (plan_maps) cudaFree(plan_maps);
         for (void *p : dev_allocs) cudaFree(p);
         if (d_out) cudaFree(d_out);
         if (d_flush) cudaFree(d_flush);
@@ -544,9 +551,12 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
 
     // device memory
     CUDA_TRY(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+    // Newton / increment-end work split: at most two 128-thread units per SM
+    // (the Newton kernel's registers allow two resident blocks per SM); the
+    // per-RVE partial sums follow this split, so it is fixed per grid size
     const long long sm_count = 152;
     long long nb = (nv + 127) / 128;
-    r->npart = (int)(nb < sm_count * 8 ? nb : sm_count * 8);
+    r->npart = (int)(nb < sm_count * 2 ? nb : sm_count * 2);
     d.npart = r->npart;
     int rc = VOCE_OK;
 #define AL(ptr, n) if ((rc = dalloc(r, ptr, (size_t)(n))) != VOCE_OK) { delete r; return rc; }
@@ -643,6 +653,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     m.first_iter = 1;
     m.active = 1;
     m.target = 0x7fffffff;
+    m.pending_prelude = 1;
     m.Err_e = 2. * d.err_tol;
     m.Err_s = 2. * d.err_tol;
     CUDA_TRY(cudaMemcpyAsync(d.macro, &m, sizeof(m), cudaMemcpyHostToDevice, r->stream));
@@ -650,7 +661,6 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     else r->tiles.choose<double>(d);
     d.zrows = r->tiles.zrows; d.yxt = r->tiles.yxt; d.xkc = r->tiles.xkc;
     d.xkc3 = r->tiles.xkc3; d.zirows = r->tiles.zirows; d.zirows3 = r->tiles.zirows3;
-    CUDA_TRY(set_smem_limits(r->precision != 0, r->tiles, d));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     *out = r;
     return VOCE_OK;
@@ -714,18 +724,68 @@ void collect_increment(voce_rve *r, const IncrDev &rec, const double *log_rows)
     r->n_done++;
 }
 
+// Work lists and descriptor array of a set of RVEs (device memory).
+int make_plan(const std::vector<RveDesc> &descs, bool mixed, RveDesc *&d_descs, int2 *&d_maps, BatchPlan &p)
+{
+    if (d_descs) cudaFree(d_descs);
+    if (d_maps) cudaFree(d_maps);
+    d_descs = nullptr;
+    d_maps = nullptr;
+    int *ticks = p.ticks, *maxt = p.max_ticks, *act = p.active_out;
+    p = BatchPlan();
+    p.ticks = ticks; p.max_ticks = maxt; p.active_out = act;
+    p.mixed = mixed;
+    p.nrve = (int)descs.size();
+    if (descs.empty()) return VOCE_OK;
+    std::vector<std::vector<int2>> maps(BP_COUNT);
+    for (int i = 0; i < p.nrve; ++i) {
+        int u[BP_COUNT];
+        batch_units(descs[i], u);
+        for (int ph = 0; ph < BP_COUNT; ++ph) {
+            for (int k = 0; k < u[ph]; ++k) maps[ph].push_back(make_int2(i, k));
+            p.smem[ph] = std::max(p.smem[ph], batch_smem(descs[i], ph));
+        }
+    }
+    size_t tot = 0;
+    for (int ph = 0; ph < BP_COUNT; ++ph) tot += maps[ph].size();
+    CUDA_TRY(cudaMalloc(&d_descs, sizeof(RveDesc) * descs.size()));
+    CUDA_TRY(cudaMalloc(&d_maps, sizeof(int2) * tot));
+    CUDA_TRY(cudaMemcpy(d_descs, descs.data(), sizeof(RveDesc) * descs.size(), cudaMemcpyHostToDevice));
+    size_t off = 0;
+    for (int ph = 0; ph < BP_COUNT; ++ph) {
+        CUDA_TRY(cudaMemcpy(d_maps + off, maps[ph].data(), sizeof(int2) * maps[ph].size(), cudaMemcpyHostToDevice));
+        p.map[ph] = d_maps + off;
+        p.total[ph] = (int)maps[ph].size();
+        off += maps[ph].size();
+    }
+    p.descs = d_descs;
+    CUDA_TRY(set_batch_smem(p));
+    return VOCE_OK;
+}
+
+int ensure_self_plan(voce_rve *r)
+{
+    if (!r->plan_dirty) return VOCE_OK;
+    std::vector<RveDesc> one(1, r->d);
+    int rc = make_plan(one, r->precision != 0, r->plan_desc, r->plan_maps, r->plan);
+    if (rc) return rc;
+    r->plan_dirty = false;
+    return VOCE_OK;
+}
+
 // One increment with the host deciding after every iteration (used when
 // profiling per kernel, and when the loop bounds are degenerate).
 int run_increment_hostloop(voce_rve *r)
 {
     RveDesc &d = r->d;
-    CUDA_TRY(launch_prelude(d, r->stream, r->prof));
+    int rc = ensure_self_plan(r);
+    if (rc) return rc;
+    CUDA_TRY(launch_plan_prelude(r->plan, r->stream, r->prof));
     int guard = 0;
     // the reference tests the loop condition before the first iteration
     const bool any = d.iter_max > 0 && 2.0 * std::fabs(d.err_tol) > std::fabs(d.err_tol);
     while (any) {
-        cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, r->prof)
-                                     : launch_iteration<double>(d, r->tiles, r->npart, r->stream, r->prof);
+        cudaError_t e = launch_plan_iteration(r->plan, r->stream, r->prof, 0, 0);
         if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "iteration launch: %s", cudaGetErrorString(e));
         CUDA_TRY(cudaMemcpyAsync(r->h_flag, &d.macro->converged, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
         CUDA_TRY(cudaStreamSynchronize(r->stream));
@@ -733,8 +793,7 @@ int run_increment_hostloop(voce_rve *r)
         if (*r->h_flag) break;
         if (++guard > d.iter_max + 1) return fail(VOCE_ERR_STATE, "iteration control lost");
     }
-    cudaError_t e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, r->prof)
-                                 : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, r->prof);
+    cudaError_t e = launch_plan_incr_end(r->plan, r->stream, r->prof);
     if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "increment-end launch: %s", cudaGetErrorString(e));
     return VOCE_OK;
 }
@@ -745,12 +804,13 @@ int run_increment_hostloop(voce_rve *r)
 // change between launches, all state lives in device memory.
 int build_graph(voce_rve *r)
 {
-    RveDesc &d = r->d;
+    int rc = ensure_self_plan(r);
+    if (rc) return rc;
     Prof none;  // no events inside graphs
     cudaGraph_t g;
     CUDA_TRY(cudaGraphCreate(&g, 0));
     CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    CUDA_TRY(launch_prelude(d, r->stream, none));
+    CUDA_TRY(launch_plan_prelude(r->plan, r->stream, none));
     CUDA_TRY(cudaStreamEndCapture(r->stream, &g));
     size_t nn = 0;
     CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
@@ -766,74 +826,15 @@ int build_graph(voce_rve *r)
     CUDA_TRY(cudaGraphAddNode(&cond, g, pre.data(), nullptr, pre.size(), &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = r->precision ? launch_iteration<float>(d, r->tiles, r->npart, r->stream, none, h, 1)
-                                 : launch_iteration<double>(d, r->tiles, r->npart, r->stream, none, h, 1);
+    cudaError_t e = launch_plan_iteration(r->plan, r->stream, none, h, 1);
     CUDA_TRY(cudaStreamEndCapture(r->stream, &body));
     CUDA_TRY(e);
     CUDA_TRY(cudaStreamBeginCaptureToGraph(r->stream, g, &cond, nullptr, 1, cudaStreamCaptureModeThreadLocal));
-    e = r->precision ? launch_increment_end<float>(d, r->sc, r->tiles, r->npart, r->stream, none)
-                     : launch_increment_end<double>(d, r->sc, r->tiles, r->npart, r->stream, none);
+    e = launch_plan_incr_end(r->plan, r->stream, none);
     CUDA_TRY(cudaStreamEndCapture(r->stream, &g));
     CUDA_TRY(e);
     CUDA_TRY(cudaGraphInstantiate(&r->graph_exec, g, 0));
     r->graph = g;
-    // launches per increment: prelude + 7 per iteration + 5 at the end
-    return VOCE_OK;
-}
-
-// Copy the records and iteration logs of the increments finished since the
-// last read-back from the device rings (capacity incr_cap increments).
-int collect_new(voce_rve *r, bool count_graph_launches)
-{
-    RveDesc &d = r->d;
-    MacroDev m;
-    CUDA_TRY(cudaMemcpyAsync(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost, r->stream));
-    CUDA_TRY(cudaStreamSynchronize(r->stream));
-    const int completed = m.istep - 1;
-    const int fresh = completed - r->n_done;
-    if (fresh <= 0) return VOCE_OK;
-    if (fresh > d.incr_cap) return fail(VOCE_ERR_STATE, "increment ring overflow (%d > %d)", fresh, d.incr_cap);
-    std::vector<IncrDev> recs(d.incr_cap);
-    std::vector<double> logs((size_t)d.incr_cap * d.iter_max * VOCE_ITLOG);
-    CUDA_TRY(cudaMemcpyAsync(recs.data(), d.incr, sizeof(IncrDev) * recs.size(), cudaMemcpyDeviceToHost, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(logs.data(), d.itlog, sizeof(double) * logs.size(), cudaMemcpyDeviceToHost, r->stream));
-    CUDA_TRY(cudaStreamSynchronize(r->stream));
-    CUDA_TRY(cudaGetLastError());
-    const int first = r->n_done;
-    for (int k = 0; k < fresh; ++k) {
-        const int slot = (first + k) % d.incr_cap;
-        if (recs[slot].istep != first + k + 1)
-            return fail(VOCE_ERR_STATE, "increment record %d missing", first + k + 1);
-        // one prelude, 7 launches per iteration, 7 at the increment end
-        if (count_graph_launches) r->prof.launches += 1 + 7LL * recs[slot].iters + 7;
-        collect_increment(r, recs[slot], logs.data() + (size_t)slot * d.iter_max * VOCE_ITLOG);
-    }
-    return VOCE_OK;
-}
-
-// Grow the record rings to hold `cap` increments (drops the cached graph,
-// whose kernel arguments point at the old rings).
-int ensure_ring(voce_rve *r, int cap)
-{
-    RveDesc &d = r->d;
-    if (cap <= d.incr_cap) return VOCE_OK;
-    int rc = collect_new(r, false);
-    if (rc) return rc;
-    double *lg = nullptr;
-    IncrDev *ic = nullptr;
-    if ((rc = dalloc(r, lg, (size_t)cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1)))) return rc;
-    if ((rc = dalloc(r, ic, (size_t)cap))) return rc;
-    // live slots keep their absolute index modulo the capacity
-    std::vector<IncrDev> old(d.incr_cap);
-    CUDA_TRY(cudaMemcpy(old.data(), d.incr, sizeof(IncrDev) * old.size(), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < d.incr_cap; ++k)
-        if (old[k].istep > 0)
-            CUDA_TRY(cudaMemcpy(ic + (old[k].istep - 1) % cap, &old[k], sizeof(IncrDev), cudaMemcpyHostToDevice));
-    d.itlog = lg;
-    d.incr = ic;
-    d.incr_cap = cap;
-    if (r->graph_exec) { cudaGraphExecDestroy(r->graph_exec); r->graph_exec = nullptr; }
-    if (r->graph) { cudaGraphDestroy(r->graph); r->graph = nullptr; }
     return VOCE_OK;
 }
 
@@ -1078,33 +1079,12 @@ int build_batch(voce_batch *b)
     p.mixed = b->precision != 0;
     if (n == 0) { b->dirty = false; return VOCE_OK; }
     std::vector<RveDesc> descs(n);
-    std::vector<std::vector<int2>> maps(BP_COUNT);
-    for (int i = 0; i < n; ++i) {
-        descs[i] = b->rves[i]->d;
-        int u[BP_COUNT];
-        batch_units(descs[i], u);
-        for (int ph = 0; ph < BP_COUNT; ++ph) {
-            for (int k = 0; k < u[ph]; ++k) maps[ph].push_back(make_int2(i, k));
-            p.smem[ph] = std::max(p.smem[ph], batch_smem(descs[i], ph));
-        }
-    }
-    size_t tot = 0;
-    for (int ph = 0; ph < BP_COUNT; ++ph) tot += maps[ph].size();
-    CUDA_TRY(cudaMalloc(&b->d_descs, sizeof(RveDesc) * n));
-    CUDA_TRY(cudaMalloc(&b->d_maps, sizeof(int2) * tot));
-    CUDA_TRY(cudaMemcpy(b->d_descs, descs.data(), sizeof(RveDesc) * n, cudaMemcpyHostToDevice));
-    size_t off = 0;
-    for (int ph = 0; ph < BP_COUNT; ++ph) {
-        CUDA_TRY(cudaMemcpy(b->d_maps + off, maps[ph].data(), sizeof(int2) * maps[ph].size(), cudaMemcpyHostToDevice));
-        p.map[ph] = b->d_maps + off;
-        p.total[ph] = (int)maps[ph].size();
-        off += maps[ph].size();
-    }
-    p.descs = b->d_descs;
+    for (int i = 0; i < n; ++i) descs[i] = b->rves[i]->d;
     p.ticks = b->d_ctl;
     p.max_ticks = b->d_ctl + 1;
     p.active_out = b->d_ctl + 2;
-    CUDA_TRY(set_batch_smem(p));
+    int rc = make_plan(descs, b->precision != 0, b->d_descs, b->d_maps, p);
+    if (rc) return rc;
     // graph: WHILE (any RVE active and ticks < max) { tick }
     cudaGraph_t g;
     CUDA_TRY(cudaGraphCreate(&g, 0));

@@ -41,27 +41,42 @@ __device__ void block_partials(double (&acc)[VOCE_NPART], double *out)
     __syncthreads();
 }
 
-// sum the per-block partials of one kernel in a fixed order (one block)
+// sum the per-block partials of one kernel in a fixed order (one block of
+// 256 threads): 16 stripes per quantity, 8 independent loads in flight per
+// thread, then the stripes in order
 __device__ void reduce_partials(const double *part, int npart, double (&tot)[VOCE_NPART])
 {
     __shared__ double red[16][VOCE_NPART];
     const int t = threadIdx.x;  // blockDim.x == 256
     const int q = t % VOCE_NPART, stripe = t / VOCE_NPART;
-    double s = (q == VOCE_NPART - 1) ? 0.0 : 0.0;
-    for (int b = stripe; b < npart; b += 16) {
-        double x = part[(long long)b * VOCE_NPART + q];
-        s = (q == VOCE_NPART - 1) ? fmax(s, x) : s + x;
+    const bool mx = q == VOCE_NPART - 1;
+    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int b = stripe;
+    for (; b + 7 * 16 < npart; b += 8 * 16) {
+        double x[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = part[(long long)(b + 16 * k) * VOCE_NPART + q];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = mx ? fmax(a[k], x[k]) : a[k] + x[k];
     }
+    for (int k = 0; b < npart; b += 16, ++k) {
+        const double x = part[(long long)b * VOCE_NPART + q];
+        a[k & 7] = mx ? fmax(a[k & 7], x) : a[k & 7] + x;
+    }
+    double s = a[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) s = mx ? fmax(s, a[k]) : s + a[k];
     red[stripe][q] = s;
     __syncthreads();
     if (t < VOCE_NPART) {
-        double a = red[0][t];
-        for (int k = 1; k < 16; ++k) a = (t == VOCE_NPART - 1) ? fmax(a, red[k][t]) : a + red[k][t];
-        red[0][t] = a;
+        double v = red[0][t];
+        for (int k = 1; k < 16; ++k) v = (t == VOCE_NPART - 1) ? fmax(v, red[k][t]) : v + red[k][t];
+        red[0][t] = v;
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < VOCE_NPART; ++k) tot[k] = red[0][k];
+    __syncthreads();
 }
 
 // rotation of the 6-vector basis: x_sample = Mr * x_crystal for the
@@ -267,8 +282,6 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_fft_z_fwd(RveDesc d, int rows) { fft_z_fwd_unit<R>(d, rows, blockIdx.x); }
 
 template <typename R>
 __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int unit)
@@ -296,8 +309,6 @@ __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int 
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_fft_y(RveDesc d, void *specp, int sign, int xt) { fft_y_unit<R>(d, specp, sign, xt, blockIdx.x); }
 
 template <typename R>
 __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
@@ -360,8 +371,6 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_fft_x_green(RveDesc d, int kc) { fft_x_green_unit<R>(d, kc, blockIdx.x); }
 
 template <typename R>
 __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, int kc, int unit)
@@ -389,8 +398,6 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_fft_x(RveDesc d, void *specp, int ncomp, int sign, int kc) { fft_x_unit<R>(d, specp, ncomp, sign, kc, blockIdx.x); }
 
 // inverse z transform (Hermitian half spectrum -> real); mode 0 adds the
 // result to the symmetric displacement gradient (evolution.c:383-394),
@@ -451,8 +458,6 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_fft_z_inv(RveDesc d, void *specp, int ncomp, int rows, int mode) { fft_z_inv_unit<R>(d, specp, ncomp, rows, mode, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // per-voxel Newton-Raphson stress update (UpdateStress, evolution.c:3-168),
@@ -606,8 +611,6 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
 
-template <bool MIXED_NR>
-__global__ void __launch_bounds__(128) k_nr(RveDesc d) { nr_unit<MIXED_NR>(d, blockIdx.x, gridDim.x); }
 
 __device__ double vm_strain(const double *t)  // VonMises, evolution.c:243-262
 {
@@ -646,7 +649,7 @@ __device__ double svm_of(const double *t9)
 
 // one thread: errors, volume averages, mixed-BC macro correction,
 // convergence decision (evolution.c:401-431, get_smacro :170-241)
-__device__ void finalize_iter_body(const RveDesc &d, int npart, cudaGraphConditionalHandle cond, int use_cond)
+__device__ void finalize_iter_body(const RveDesc &d, int npart)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
@@ -702,7 +705,6 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart, cudaGraphConditi
     m->pending_prelude = 0;
     const bool more = (m->iter < d.iter_max) && (fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
     m->converged = more ? 0 : 1;
-    if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
     if (!more) {
         // epilogue macro bookkeeping (evolution.c:438-461)
         double act[9], vga[9];
@@ -733,10 +735,6 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart, cudaGraphConditi
     }
 }
 
-__global__ void k_finalize_iter(RveDesc d, int npart, cudaGraphConditionalHandle cond, int use_cond)
-{
-    finalize_iter_body(d, npart, cond, use_cond);
-}
 
 // Harden one voxel: harden() body (constitutive.c:261-305)
 __device__ void harden_voxel(const RveDesc &d, long long v, const double *gd)
@@ -924,7 +922,6 @@ __device__ void incr_end_unit(const RveDesc &d, int unit, int nunits)
     block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
 
-__global__ void __launch_bounds__(128) k_incr_end(RveDesc d) { incr_end_unit(d, blockIdx.x, gridDim.x); }
 
 // increment prelude (evolution.c:306-318): DisGrad += Udot dt, or, under
 // creep, DisGrad := DisGradAvg_actual of the previous increment
@@ -946,7 +943,6 @@ __device__ void prelude_unit(const RveDesc &d, int unit, int nunits)
         }
 }
 
-__global__ void k_prelude(RveDesc d) { prelude_unit(d, blockIdx.x, gridDim.x); }
 
 __device__ void finalize_incr_body(const RveDesc &d, int npart)
 {
@@ -1006,7 +1002,6 @@ __device__ void finalize_incr_body(const RveDesc &d, int npart)
     for (int q = 0; q < 3; ++q) m->acum_a[q] = 0.0;
 }
 
-__global__ void k_finalize_incr(RveDesc d, int npart) { finalize_incr_body(d, npart); }
 
 // fields in the reference's layouts, for download
 __global__ void k_field_out(RveDesc d, int field, double *out)
@@ -1177,14 +1172,18 @@ __global__ void __launch_bounds__(128) kb_prelude(const RveDesc *descs, const in
     }
 }
 
-// one block per RVE
-__global__ void __launch_bounds__(256) kb_finalize(const RveDesc *descs, int nrve, int incr_end)
+// one block per RVE.  With use_cond (a plan of one RVE), the iteration
+// finaliser also sets the condition of the graph's WHILE node: continue
+// while the RVE has not converged (evolution.c:342).
+__global__ void __launch_bounds__(256) kb_finalize(const RveDesc *descs, int nrve, int incr_end,
+                                                   cudaGraphConditionalHandle cond, int use_cond)
 {
     for (int r = blockIdx.x; r < nrve; r += gridDim.x) {
         const RveDesc &d = descs[r];
         if (!unit_on(d, incr_end ? MASK_CONVERGED : MASK_ACTIVE)) continue;
         if (incr_end) finalize_incr_body(d, d.npart);
-        else finalize_iter_body(d, d.npart, 0, 0);
+        else finalize_iter_body(d, d.npart);
+        if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(cond, d.macro->converged ? 0u : 1u);
         __syncthreads();
     }
 }
@@ -1235,95 +1234,12 @@ void Tiles::choose(const RveDesc &d)
 template void Tiles::choose<double>(const RveDesc &);
 template void Tiles::choose<float>(const RveDesc &);
 
+
 template <typename R>
 static size_t smem_lines(int L, int NL)
 {
     return (size_t)2 * L * (size_t)(NL | 1) * sizeof(typename Cx<R>::T);
 }
-
-template <typename R>
-static cudaError_t set_smem(const void *fn, size_t bytes)
-{
-    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
-template <typename R>
-static void set_smem_one(const void *fn, size_t bytes)
-{
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
-template <typename R>
-static cudaError_t set_smem_all(const Tiles &t, const RveDesc &d)
-{
-    set_smem_one<R>((const void *)k_fft_z_fwd<R>, smem_lines<R>(d.nz, 3 * t.zrows));
-    set_smem_one<R>((const void *)k_fft_y<R>, smem_lines<R>(d.ny, t.yxt));
-    set_smem_one<R>((const void *)k_fft_x_green<R>, smem_lines<R>(d.nx, 6 * t.xkc));
-    set_smem_one<R>((const void *)k_fft_x<R>, smem_lines<R>(d.nx, 3 * t.xkc3));
-    size_t zi = smem_lines<R>(d.nz, 3 * t.zirows), zi3 = smem_lines<R>(d.nz, 2 * t.zirows3);
-    set_smem_one<R>((const void *)k_fft_z_inv<R>, zi > zi3 ? zi : zi3);
-    return cudaGetLastError();
-}
-
-cudaError_t set_smem_limits(bool mixed, const Tiles &t, const RveDesc &d)
-{
-    return mixed ? set_smem_all<float>(t, d) : set_smem_all<double>(t, d);
-}
-
-template <typename R>
-cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf,
-                             cudaGraphConditionalHandle cond, int use_cond)
-{
-    pf.begin(K_FFT_Z_FWD, s);
-    k_fft_z_fwd<R><<<d.nx * (d.ny / t.zrows), 256, smem_lines<R>(d.nz, 3 * t.zrows), s>>>(d, t.zrows);
-    pf.end(K_FFT_Z_FWD, s);
-    pf.begin(K_FFT_Y_FWD, s);
-    k_fft_y<R><<<6 * d.nzh * (d.nx / t.yxt), 256, smem_lines<R>(d.ny, t.yxt), s>>>(d, d.spec, -1, t.yxt);
-    pf.end(K_FFT_Y_FWD, s);
-    pf.begin(K_FFT_X_GREEN, s);
-    k_fft_x_green<R><<<d.nzh * (d.ny / t.xkc), 256, smem_lines<R>(d.nx, 6 * t.xkc), s>>>(d, t.xkc);
-    pf.end(K_FFT_X_GREEN, s);
-    pf.begin(K_FFT_Y_INV, s);
-    k_fft_y<R><<<6 * d.nzh * (d.nx / t.yxt), 256, smem_lines<R>(d.ny, t.yxt), s>>>(d, d.spec, +1, t.yxt);
-    pf.end(K_FFT_Y_INV, s);
-    pf.begin(K_FFT_Z_INV, s);
-    k_fft_z_inv<R><<<d.nx * (d.ny / t.zirows), 256, smem_lines<R>(d.nz, 3 * t.zirows), s>>>(d, d.spec, 6, t.zirows, 0);
-    pf.end(K_FFT_Z_INV, s);
-    pf.begin(K_NR, s);
-    if (d.mixed) k_nr<true><<<npart, 128, 0, s>>>(d);
-    else k_nr<false><<<npart, 128, 0, s>>>(d);
-    pf.end(K_NR, s);
-    pf.begin(K_FIN_ITER, s);
-    k_finalize_iter<<<1, 256, 0, s>>>(d, npart, cond, use_cond);
-    pf.end(K_FIN_ITER, s);
-    return cudaGetLastError();
-}
-template cudaError_t launch_iteration<double>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &,
-                                             cudaGraphConditionalHandle, int);
-template cudaError_t launch_iteration<float>(const RveDesc &, const Tiles &, int, cudaStream_t, Prof &,
-                                            cudaGraphConditionalHandle, int);
-
-template <typename R>
-cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,
-                                 cudaStream_t s, Prof &pf)
-{
-    pf.begin(K_INC_FFT, s);
-    k_fft_x<R><<<d.nzh * (d.ny / t.xkc3), 256, smem_lines<R>(d.nx, 3 * t.xkc3), s>>>(d, d.aacc, 3, +1, t.xkc3);
-    k_fft_y<R><<<3 * d.nzh * (d.nx / t.yxt), 256, smem_lines<R>(d.ny, t.yxt), s>>>(d, d.aacc, +1, t.yxt);
-    k_fft_z_inv<R><<<d.nx * (d.ny / t.zirows3), 256, smem_lines<R>(d.nz, 2 * t.zirows3), s>>>(d, d.aacc, 3, t.zirows3, 1);
-    pf.end(K_INC_FFT, s, 3);
-    pf.begin(K_INCR_END, s);
-    k_incr_end<<<npart, 128, 0, s>>>(d);
-    pf.end(K_INCR_END, s);
-    pf.begin(K_FIN_INCR, s);
-    k_finalize_incr<<<1, 256, 0, s>>>(d, npart);
-    pf.end(K_FIN_INCR, s);
-    return cudaGetLastError();
-}
-template cudaError_t launch_increment_end<double>(const RveDesc &, const SetupConst &, const Tiles &, int,
-                                                  cudaStream_t, Prof &);
-template cudaError_t launch_increment_end<float>(const RveDesc &, const SetupConst &, const Tiles &, int,
-                                                 cudaStream_t, Prof &);
 
 void batch_units(const RveDesc &d, int u[BP_COUNT])
 {
@@ -1381,31 +1297,91 @@ static int grid_for(int total, int cap)
 }
 
 template <typename R>
-static void batch_tick_t(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond)
+static void plan_prelude_t(const BatchPlan &bp, cudaStream_t s, Prof &pf)
+{
+    const int NG = 152 * 2;
+    pf.begin(K_PRELUDE, s);
+    kb_prelude<<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(bp.descs, bp.map[BP_NP], bp.total[BP_NP]);
+    pf.end(K_PRELUDE, s);
+}
+
+template <typename R>
+static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cudaGraphConditionalHandle cond,
+                             int use_cond)
 {
     const int FG = 152 * 4, NG = 152 * 2;
     const RveDesc *D = bp.descs;
-    kb_prelude<<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    pf.begin(K_FFT_Z_FWD, s);
     kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
+    pf.end(K_FFT_Z_FWD, s);
+    pf.begin(K_FFT_Y_FWD, s);
     kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0);
+    pf.end(K_FFT_Y_FWD, s);
+    pf.begin(K_FFT_X_GREEN, s);
     kb_fft_x_green<R><<<grid_for(bp.total[BP_XG], FG), 256, bp.smem[BP_XG], s>>>(D, bp.map[BP_XG], bp.total[BP_XG]);
+    pf.end(K_FFT_X_GREEN, s);
+    pf.begin(K_FFT_Y_INV, s);
     kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 1);
+    pf.end(K_FFT_Y_INV, s);
+    pf.begin(K_FFT_Z_INV, s);
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
+    pf.end(K_FFT_Z_INV, s);
+    pf.begin(K_NR, s);
     if (bp.mixed) kb_nr<true><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
     else kb_nr<false><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
-    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 0);
+    pf.end(K_NR, s);
+    pf.begin(K_FIN_ITER, s);
+    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 0, cond, use_cond);
+    pf.end(K_FIN_ITER, s);
+}
+
+template <typename R>
+static void plan_incr_end_t(const BatchPlan &bp, cudaStream_t s, Prof &pf)
+{
+    const int FG = 152 * 4, NG = 152 * 2;
+    const RveDesc *D = bp.descs;
+    pf.begin(K_INC_FFT, s);
     kb_fft_x_aacc<R><<<grid_for(bp.total[BP_X3], FG), 256, bp.smem[BP_X3], s>>>(D, bp.map[BP_X3], bp.total[BP_X3]);
     kb_fft_y<R><<<grid_for(bp.total[BP_Y3], FG), 256, bp.smem[BP_Y3], s>>>(D, bp.map[BP_Y3], bp.total[BP_Y3], 2);
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_Z3], FG), 256, bp.smem[BP_Z3], s>>>(D, bp.map[BP_Z3], bp.total[BP_Z3], 1);
+    pf.end(K_INC_FFT, s, 3);
+    pf.begin(K_INCR_END, s);
     kb_incr_end<<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
-    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 1);
-    kb_cond<<<1, 256, 0, s>>>(D, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, cond);
+    pf.end(K_INCR_END, s);
+    pf.begin(K_FIN_INCR, s);
+    kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 1, 0, 0);
+    pf.end(K_FIN_INCR, s);
+}
+
+cudaError_t launch_plan_prelude(const BatchPlan &bp, cudaStream_t s, Prof &pf)
+{
+    if (bp.mixed) plan_prelude_t<float>(bp, s, pf);
+    else plan_prelude_t<double>(bp, s, pf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plan_iteration(const BatchPlan &bp, cudaStream_t s, Prof &pf,
+                                  cudaGraphConditionalHandle cond, int use_cond)
+{
+    if (bp.mixed) plan_iteration_t<float>(bp, s, pf, cond, use_cond);
+    else plan_iteration_t<double>(bp, s, pf, cond, use_cond);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plan_incr_end(const BatchPlan &bp, cudaStream_t s, Prof &pf)
+{
+    if (bp.mixed) plan_incr_end_t<float>(bp, s, pf);
+    else plan_incr_end_t<double>(bp, s, pf);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond)
 {
-    if (bp.mixed) batch_tick_t<float>(bp, s, cond);
-    else batch_tick_t<double>(bp, s, cond);
+    Prof none;
+    launch_plan_prelude(bp, s, none);
+    launch_plan_iteration(bp, s, none, 0, 0);
+    launch_plan_incr_end(bp, s, none);
+    kb_cond<<<1, 256, 0, s>>>(bp.descs, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, cond);
     return cudaGetLastError();
 }
 
@@ -1416,15 +1392,6 @@ cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *e
     return cudaGetLastError();
 }
 
-cudaError_t launch_prelude(const RveDesc &d, cudaStream_t s, Prof &pf)
-{
-    int blocks = (int)((d.nv + 255) / 256);
-    if (blocks > 4096) blocks = 4096;
-    pf.begin(K_PRELUDE, s);
-    k_prelude<<<blocks, 256, 0, s>>>(d);
-    pf.end(K_PRELUDE, s);
-    return cudaGetLastError();
-}
 
 // writes n doubles: evicts the L2 between timed steps
 __global__ void k_flush(double *buf, long long n)

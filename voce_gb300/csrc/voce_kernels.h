@@ -49,13 +49,6 @@ struct Prof {
     }
 };
 
-template <typename R>
-cudaError_t launch_iteration(const RveDesc &d, const Tiles &t, int npart, cudaStream_t s, Prof &pf,
-                             cudaGraphConditionalHandle cond = 0, int use_cond = 0);
-template <typename R>
-cudaError_t launch_increment_end(const RveDesc &d, const SetupConst &sc, const Tiles &t, int npart,
-                                 cudaStream_t s, Prof &pf);
-cudaError_t set_smem_limits(bool mixed, const Tiles &t, const RveDesc &d);
 
 // Work lists of one batch (device memory): per phase, (rve, unit) pairs.
 enum BatchPhase {
@@ -78,11 +71,17 @@ cudaError_t set_batch_smem(const BatchPlan &bp);
 // one tick: prelude (pending), one Green iteration of every active RVE, the
 // increment end of every RVE that converged, the loop condition
 cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond);
+// The phases of a plan (a lone RVE runs as a plan of one, with the same
+// kernels as any batch): prelude; one Green iteration, whose finaliser sets
+// the WHILE condition when use_cond; the increment end.
+cudaError_t launch_plan_prelude(const BatchPlan &bp, cudaStream_t s, Prof &pf);
+cudaError_t launch_plan_iteration(const BatchPlan &bp, cudaStream_t s, Prof &pf,
+                                  cudaGraphConditionalHandle cond, int use_cond);
+cudaError_t launch_plan_incr_end(const BatchPlan &bp, cudaStream_t s, Prof &pf);
 cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
 double measure_fp64_tflops();
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s);
-cudaError_t launch_prelude(const RveDesc &d, cudaStream_t s, Prof &pf);
 cudaError_t launch_field_out(const RveDesc &d, int field, double *out, cudaStream_t s);
 
 }  // namespace voce
