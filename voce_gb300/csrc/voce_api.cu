@@ -838,6 +838,63 @@ int build_graph(voce_rve *r)
     return VOCE_OK;
 }
 
+// Copy the records and iteration logs of the increments finished since the
+// last read-back from the device rings (capacity incr_cap increments).
+int collect_new(voce_rve *r, bool count_graph_launches)
+{
+    RveDesc &d = r->d;
+    MacroDev m;
+    CUDA_TRY(cudaMemcpyAsync(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    const int completed = m.istep - 1;
+    const int fresh = completed - r->n_done;
+    if (fresh <= 0) return VOCE_OK;
+    if (fresh > d.incr_cap) return fail(VOCE_ERR_STATE, "increment ring overflow (%d > %d)", fresh, d.incr_cap);
+    std::vector<IncrDev> recs(d.incr_cap);
+    std::vector<double> logs((size_t)d.incr_cap * d.iter_max * VOCE_ITLOG);
+    CUDA_TRY(cudaMemcpyAsync(recs.data(), d.incr, sizeof(IncrDev) * recs.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(logs.data(), d.itlog, sizeof(double) * logs.size(), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    CUDA_TRY(cudaGetLastError());
+    const int first = r->n_done;
+    for (int k = 0; k < fresh; ++k) {
+        const int slot = (first + k) % d.incr_cap;
+        if (recs[slot].istep != first + k + 1)
+            return fail(VOCE_ERR_STATE, "increment record %d missing", first + k + 1);
+        // one prelude, 7 launches per iteration, 7 at the increment end
+        if (count_graph_launches) r->prof.launches += 1 + 7LL * recs[slot].iters + 7;
+        collect_increment(r, recs[slot], logs.data() + (size_t)slot * d.iter_max * VOCE_ITLOG);
+    }
+    return VOCE_OK;
+}
+
+// Grow the record rings to hold `cap` increments (drops the cached graph
+// and plan, whose kernel arguments point at the old rings).
+int ensure_ring(voce_rve *r, int cap)
+{
+    RveDesc &d = r->d;
+    if (cap <= d.incr_cap) return VOCE_OK;
+    int rc = collect_new(r, false);
+    if (rc) return rc;
+    double *lg = nullptr;
+    IncrDev *ic = nullptr;
+    if ((rc = dalloc(r, lg, (size_t)cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1)))) return rc;
+    if ((rc = dalloc(r, ic, (size_t)cap))) return rc;
+    // live slots keep their absolute index modulo the capacity
+    std::vector<IncrDev> old(d.incr_cap);
+    CUDA_TRY(cudaMemcpy(old.data(), d.incr, sizeof(IncrDev) * old.size(), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < d.incr_cap; ++k)
+        if (old[k].istep > 0)
+            CUDA_TRY(cudaMemcpy(ic + (old[k].istep - 1) % cap, &old[k], sizeof(IncrDev), cudaMemcpyHostToDevice));
+    d.itlog = lg;
+    d.incr = ic;
+    d.incr_cap = cap;
+    if (r->graph_exec) { cudaGraphExecDestroy(r->graph_exec); r->graph_exec = nullptr; }
+    if (r->graph) { cudaGraphDestroy(r->graph); r->graph = nullptr; }
+    r->plan_dirty = true;
+    return VOCE_OK;
+}
+
 }  // namespace
 
 int voce_rve_run(voce_rve *r, int n)
