@@ -1209,7 +1209,8 @@ int voce_batch_remove(voce_batch *b, voce_rve *r)
     if (m.active && m.iter != 0) return fail(VOCE_ERR_STATE, "the RVE is in the middle of an increment");
     int rc = collect_new(r, false);
     if (rc) return rc;
-    rc = set_macro_flags(r, 1, 0x7fffffff, 0);
+    // between increments the next increment's prelude has not run yet
+    rc = set_macro_flags(r, 1, 0x7fffffff, 1);
     if (rc) return rc;
     b->rves.erase(std::find(b->rves.begin(), b->rves.end(), r));
     r->batch = nullptr;
@@ -1257,7 +1258,7 @@ int voce_batch_destroy(voce_batch *b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (voce_rve *r : b->rves) {
         collect_new(r, false);
-        set_macro_flags(r, 1, 0x7fffffff, 0);
+        set_macro_flags(r, 1, 0x7fffffff, 1);
         r->batch = nullptr;
     }
     delete b;
