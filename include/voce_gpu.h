@@ -160,6 +160,32 @@ int voce_rve_get_iter_log(const voce_rve *r, int k, double *err_e,
  * voxels of the stress 6-vector.  Returns the number of rows written. */
 int voce_rve_get_iter_detail(const voce_rve *r, int k, double *rows, int max);
 int voce_rve_get_field(voce_rve *r, int field, double *host_out);
+
+/* voce_rve_get_field_noalloc: voce_rve_get_field without any device
+ * allocation.  It has no counterpart in the reference (whose fields are host
+ * globals).  For callers that cannot allocate device memory at download time:
+ * a server whose HBM budget is committed to admitted RVEs (it downloads a
+ * finished request before freeing that request's memory), a host that
+ * overlaps downloads with other RVEs' increments on other streams (cudaMalloc
+ * and cudaFree can synchronise the whole device), a host whose device memory
+ * all belongs to its own pool allocator.  It calls no cudaMalloc, cudaFree or
+ * other allocating routine; the field is staged in a fixed array of
+ * VOCE_NOALLOC_MAX_DOUBLES doubles (32 MiB) that every GPU loading this
+ * library's device code holds until the process exits.
+ *   - A field of more doubles (width x voxels) fails with
+ *     VOCE_ERR_UNSUPPORTED; voce_rve_get_field has no such limit.  Every field
+ *     of an RVE up to 64^3 fits, and 1-wide fields up to 4 Mi voxels.
+ *   - The first call on a device does its set-up (looks up the array's device
+ *     address); make that first call before any stream capture.
+ *   - All calls on a device share the array, which keeps the last call's
+ *     contents.  Each call writes every value it reads back, so nothing needs
+ *     clearing, but calls whose work overlaps on the GPU (threads downloading
+ *     RVEs on different streams at once) race on it: serialise them.
+ *   - Output, errors and the synchronisation on return are those of
+ *     voce_rve_get_field. */
+#define VOCE_NOALLOC_MAX_DOUBLES 4194304
+int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out);
+
 int voce_rve_destroy(voce_rve *r);
 
 /* Device-memory footprint of an RVE of the given grid and precision, in

@@ -21,6 +21,7 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
           5: "ERR_SINGULAR", 6: "ERR_UNSUPPORTED", 7: "ERR_NOMEM", 8: "ERR_CUDA",
           9: "ERR_STATE"}
 PREC_FP64, PREC_MIXED = 0, 1
+NOALLOC_MAX_DOUBLES = 4194304   # VOCE_NOALLOC_MAX_DOUBLES
 FIELD = {"sig": 0, "eps": 1, "edot": 2, "disgrad": 3, "tranmat": 4, "crss": 5,
          "gamdot": 6, "gamacum": 7, "svm": 8, "evm": 9, "sig_voigt": 20,
          "edot_voigt": 21}
@@ -96,6 +97,7 @@ PROTOTYPES = [
                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
     ("voce_rve_get_iter_detail", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     ("voce_rve_get_field", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_rve_get_field_noalloc", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     ("voce_rve_destroy", C.c_int, [C.c_void_p]),
     ("voce_rve_footprint", C.c_longlong, [C.POINTER(C.c_int), C.c_int]),
     # voce_gpu_diag.h
@@ -299,6 +301,18 @@ class Rve:
         w = FIELD_WIDTH[fid]
         out = np.zeros(self.nv * w)
         _check(load().voce_rve_get_field(self._h, fid, _dptr(out)))
+        if fid in (20, 21):
+            return out.reshape(w, self.nv)
+        return out.reshape(self.nv, w)
+
+    def field_noalloc(self, name: str) -> np.ndarray:
+        """field() through voce_rve_get_field_noalloc: staged in the library's
+        fixed device array, no device allocation; VoceError ERR_UNSUPPORTED
+        when the field has more than NOALLOC_MAX_DOUBLES values."""
+        fid = FIELD[name]
+        w = FIELD_WIDTH[fid]
+        out = np.zeros(self.nv * w)
+        _check(load().voce_rve_get_field_noalloc(self._h, fid, _dptr(out)))
         if fid in (20, 21):
             return out.reshape(w, self.nv)
         return out.reshape(self.nv, w)

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -974,6 +975,92 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out)
     CUDA_TRY(cudaMemcpyAsync(host_out, r->d_out, sizeof(double) * per * r->d.nv, cudaMemcpyDeviceToHost, r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     return VOCE_OK;
+}
+
+}  // extern "C"
+
+// ---- field download without device allocation -----------------------------
+// voce_rve_get_field stages a field in a buffer it cudaMallocs on first use.
+// Callers that cannot allocate use voce_rve_get_field_noalloc instead, which
+// stages in the fixed array below: a server whose HBM budget is committed to
+// admitted RVEs when it downloads a finished request (the download comes
+// before that request's memory is freed), a host that overlaps downloads with
+// other RVEs' increments on other streams (cudaMalloc and cudaFree can
+// synchronise the whole device), and hosts that hand all device memory to
+// their own pool allocator.  The array is 32 MiB on every GPU that loads this
+// library's device code, held until the process exits.
+static __device__ __align__(256) double g_field_stage[VOCE_NOALLOC_MAX_DOUBLES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_stage_mu;
+double *g_stage_ptr[kMaxDevices] = {};
+
+// Device address of g_field_stage on device dev, which must be current.  The
+// host-side name is only a stand-in for the symbol, so the address is asked
+// for once per device and kept.
+int stage_address(int dev, double **out)
+{
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(VOCE_ERR_UNSUPPORTED, "device %d: no staging array above device %d", dev,
+                    kMaxDevices - 1);
+    std::lock_guard<std::mutex> lock(g_stage_mu);
+    if (!g_stage_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_field_stage);
+        if (e != cudaSuccess || !p)
+            return fail(VOCE_ERR_CUDA, "cudaGetSymbolAddress(g_field_stage) on device %d: %s", dev,
+                        cudaGetErrorString(e));
+        g_stage_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_stage_ptr[dev];
+    return VOCE_OK;
+}
+
+int noalloc_download(voce_rve *r, int field, long long n, int dev, double *host_out)
+{
+    double *stage = nullptr;
+    int rc = stage_address(dev, &stage);
+    if (rc) return rc;
+    // k_field_out writes each of the n doubles read back below, so nothing in
+    // the array has to start at zero; what lies past n keeps an earlier call's
+    // values and is never read.
+    CUDA_TRY(launch_field_out(r->d, field, stage, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(host_out, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return VOCE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out)
+{
+    if (!r || !host_out) return fail(VOCE_ERR_ARG, "null argument");
+    int per;
+    switch (field) {
+    case 0: case 1: case 2: case 3: case 4: per = 9; break;
+    case 5: case 6: per = 12; break;
+    case 7: case 8: case 9: per = 1; break;
+    case 20: case 21: per = 6; break;
+    default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
+    }
+    const long long n = (long long)per * r->d.nv;
+    if (n > VOCE_NOALLOC_MAX_DOUBLES)
+        return fail(VOCE_ERR_UNSUPPORTED,
+                    "field %d of %lld voxels is %lld doubles, more than the %d doubles of the "
+                    "no-allocation staging array; use voce_rve_get_field",
+                    field, (long long)r->d.nv, n, VOCE_NOALLOC_MAX_DOUBLES);
+    // the RVE's stream names its device; run there and restore the caller's
+    int dev = 0, cur = 0;
+    CUDA_TRY(cudaStreamGetDevice(r->stream, &dev));
+    CUDA_TRY(cudaGetDevice(&cur));
+    if (dev != cur) CUDA_TRY(cudaSetDevice(dev));
+    int rc = noalloc_download(r, field, n, dev, host_out);
+    if (dev != cur) cudaSetDevice(cur);
+    return rc;
 }
 
 int voce_rve_destroy(voce_rve *r)
