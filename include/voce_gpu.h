@@ -120,6 +120,11 @@ enum {
     VOCE_FIELD_GAMACUM = 7,    /* gamacum, 1 */
     VOCE_FIELD_SVM = 8,        /* SVM, 1 */
     VOCE_FIELD_EVM = 9,        /* EVM, 1 */
+    VOCE_FIELD_GAMMATOTAL = 10, /* gammatotal (shear summed over increments), 12 */
+    VOCE_FIELD_TAUX = 11,      /* tau_x (constitutive.c:45), 12 */
+    VOCE_FIELD_RHO_RSS = 12,   /* rho_rss  (evolution.c:509-529: updated by  */
+    VOCE_FIELD_RHO_CRSS = 13,  /* rho_crss  each increment from the third on */
+    VOCE_FIELD_WORK_P = 14,    /* work_p    when Hard_Flag is 1; 0 before), 1 */
     VOCE_FIELD_SIG_VOIGT = 20, /* Sig 11,22,33,23,13,12: the order of the
                                   sig_1..6 dumps (io.c:321-358), 6 */
     VOCE_FIELD_EDOT_VOIGT = 21 /* Edot in the same order (io.c:360-397), 6 */

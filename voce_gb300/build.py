@@ -2,7 +2,8 @@
 
 ``python -m voce_gb300.build`` (or ``voce_gb300.build.build()``) compiles
 every translation unit under csrc/ with nvcc for ``sm_103a`` in parallel and
-links ``voce_gb300/lib/libvoce_gpu.so``.  No cmake, no torch extension
+links ``voce_gb300/lib/libvoce_gpu.so``, then the host-only legacy layer
+``voce_gb300/lib/libvoce_legacy.so`` on top of it.  No cmake, no torch extension
 machinery: the library has a plain C ABI (include/voce_gpu.h).
 """
 from __future__ import annotations
@@ -23,7 +24,10 @@ LIB = os.path.join(LIBDIR, "libvoce_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-SOURCES = ["voce_kernels.cu", "voce_api.cu", "voce_server.cpp"]
+SOURCES = ["voce_kernels.cu", "voce_api.cu", "voce_server.cpp", "voce_io.cpp"]
+LEGACY = os.path.join(CSRC, "legacy")
+LEGACY_SOURCES = ["voce_legacy.cpp", "voce_legacy_cxx.cpp"]
+LEGACY_LIB = os.path.join(LIBDIR, "libvoce_legacy.so")
 
 
 def _nvcc() -> str:
@@ -44,8 +48,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = _nvcc()
+    inc = os.path.join(ROOT, "include")
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(ROOT, "include", "voce_gpu.h"))
+    headers += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     jobs = []
     objs = []
     for src in SOURCES:
@@ -67,7 +72,28 @@ def build(verbose: bool = False, force: bool = False) -> str:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    build_legacy(verbose, force)
     return LIB
+
+
+def build_legacy(verbose: bool = False, force: bool = False) -> str:
+    """libvoce_legacy.so (include/voce_legacy.h): host C++ only, linked
+    against libvoce_gpu.so; its undefined symbols are the reference program's
+    globals, resolved when a program defining them loads it."""
+    srcs = [os.path.join(LEGACY, f) for f in LEGACY_SOURCES]
+    deps = srcs + [os.path.join(LEGACY, "voce_legacy_impl.h"), LIB] + [
+        os.path.join(ROOT, "include", h) for h in ("voce_gpu.h", "voce_io.h", "voce_legacy.h")]
+    if not (force or _stale(LEGACY_LIB, deps)):
+        return LEGACY_LIB
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", "-I" + os.path.join(ROOT, "include"),
+           *srcs, "-L" + LIBDIR, "-lvoce_gpu", "-Wl,-rpath,$ORIGIN", "-o", LEGACY_LIB]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("legacy build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return LEGACY_LIB
 
 
 if __name__ == "__main__":

@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libvoce_gpu.so")
+LEGACY_LIB_PATH = os.path.join(HERE, "lib", "libvoce_legacy.so")
 
 VOCE_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
@@ -22,11 +23,16 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
           9: "ERR_STATE"}
 PREC_FP64, PREC_MIXED = 0, 1
 NOALLOC_MAX_DOUBLES = 4194304   # VOCE_NOALLOC_MAX_DOUBLES
+# .iout dump kinds (include/voce_io.h)
+IOUT = {"eps": 0, "sig": 1, "els": 2, "edot": 3, "slip": 4, "taux": 5, "crss": 6, "tex": 7,
+        "svm": 8, "evm": 9, "rho_rss": 10, "rho_crss": 11, "work_p": 12, "work_e": 13,
+        "new_position": 14}
 FIELD = {"sig": 0, "eps": 1, "edot": 2, "disgrad": 3, "tranmat": 4, "crss": 5,
-         "gamdot": 6, "gamacum": 7, "svm": 8, "evm": 9, "sig_voigt": 20,
-         "edot_voigt": 21}
+         "gamdot": 6, "gamacum": 7, "svm": 8, "evm": 9, "gammatotal": 10,
+         "taux": 11, "rho_rss": 12, "rho_crss": 13, "work_p": 14,
+         "sig_voigt": 20, "edot_voigt": 21}
 FIELD_WIDTH = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 12, 7: 1, 8: 1, 9: 1,
-               20: 6, 21: 6}
+               10: 12, 11: 12, 12: 1, 13: 1, 14: 1, 20: 6, 21: 6}
 
 
 class VoceNamelist(C.Structure):
@@ -98,6 +104,13 @@ PROTOTYPES = [
     ("voce_rve_get_iter_detail", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     ("voce_rve_get_field", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     ("voce_rve_get_field_noalloc", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    ("voce_rve_write_iout", C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
+    ("voce_rve_write_step_iout", C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
+    ("voce_rve_write_final_iout", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("voce_write_log_headers", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("voce_rve_write_log", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("voce_rve_get_ids", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("voce_rve_get_namelist", C.c_int, [C.c_void_p, C.POINTER(VoceNamelist)]),
     ("voce_rve_destroy", C.c_int, [C.c_void_p]),
     ("voce_rve_footprint", C.c_longlong, [C.POINTER(C.c_int), C.c_int]),
     # voce_gpu_diag.h
@@ -316,6 +329,46 @@ class Rve:
         if fid in (20, 21):
             return out.reshape(w, self.nv)
         return out.reshape(self.nv, w)
+
+    def ids(self):
+        """Grain and phase id of every voxel."""
+        g = np.zeros(self.nv, dtype=np.int32)
+        p = np.zeros(self.nv, dtype=np.int32)
+        _check(load().voce_rve_get_ids(self._h, _iptr(g), _iptr(p)))
+        return g, p
+
+    def namelist(self) -> "VoceNamelist":
+        nl = VoceNamelist()
+        _check(load().voce_rve_get_namelist(self._h, C.byref(nl)))
+        return nl
+
+    def write_iout(self, kind: str, name: str, step: int) -> None:
+        _check(load().voce_rve_write_iout(self._h, IOUT[kind], name.encode(), step))
+
+    def write_step_iout(self, istep: int, directory: str = "") -> None:
+        _check(load().voce_rve_write_step_iout(self._h, istep, directory.encode()))
+
+    def write_final_iout(self, directory: str = "") -> None:
+        _check(load().voce_rve_write_final_iout(self._h, directory.encode()))
+
+    def write_logs(self, directory: str, n_steps: int) -> None:
+        """vm.out and err.out of every finished increment, as the reference
+        writes them for a run of n_steps increments."""
+        libc = C.CDLL(None)
+        libc.fopen.restype = C.c_void_p
+        libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+        libc.fclose.argtypes = [C.c_void_p]
+        vm = libc.fopen(os.path.join(directory, "vm.out").encode(), b"w+")
+        err = libc.fopen(os.path.join(directory, "err.out").encode(), b"w+")
+        if not vm or not err:
+            raise OSError("cannot open vm.out / err.out in " + directory)
+        try:
+            _check(load().voce_write_log_headers(vm, err))
+            for k in range(self.increments_done):
+                _check(load().voce_rve_write_log(self._h, k, n_steps, vm, err))
+        finally:
+            libc.fclose(vm)
+            libc.fclose(err)
 
     def close(self) -> None:
         if self._h:

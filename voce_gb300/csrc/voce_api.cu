@@ -3,7 +3,9 @@
 #include "voce_gpu.h"
 #include "voce_gpu_diag.h"
 #include "voce_batch.h"
+#include "voce_io.h"
 #include "voce_kernels.h"
+#include "voce_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -33,6 +35,17 @@ int fail(int code, const char *fmt, ...)
     g_err = buf;
     return code;
 }
+
+}  // namespace
+
+// error reporting for the other host translation units (voce_internal.h)
+int voce::set_error(int code, const char *msg)
+{
+    g_err = msg;
+    return code;
+}
+
+namespace {
 
 #define CUDA_TRY(x)                                                                        \
     do {                                                                                   \
@@ -198,6 +211,8 @@ struct voce_rve {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int n_done = 0, n_steps = 0;
+    std::vector<int> grain, phase;  // mesh ids, for the .iout records
+    voce_namelist nl{};
     std::vector<voce_increment> incr;
     std::vector<std::vector<double>> itlog;
     ~voce_rve()
@@ -400,8 +415,8 @@ long long voce_rve_footprint(const int dims[3], int precision)
     const long long cplx = precision == VOCE_PREC_MIXED ? 8 : 16;
     // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
-    // svm 1, evm 1, rotl 3  (= 211) + phase (4 bytes)
-    return nv * (211 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 240 : 0)) + nspec * 9 * cplx;
+    // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
+    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 240 : 0)) + nspec * 9 * cplx;
 }
 
 // ---------------------------------------------------------------------------
@@ -564,7 +579,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     AL(d.sig, 6 * nv); AL(d.sigp, 6 * nv); AL(d.eps, 5 * nv); AL(d.dgs, 6 * nv); AL(d.dga, 3 * nv);
     AL(d.tm, 9 * nv); AL(d.sch, 60 * nv); AL(d.sg, 21 * nv); AL(d.crss, 24 * nv); AL(d.itau, 24 * nv);
     AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
-    AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.phase, nv);
+    AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.diag, 3 * nv); AL(d.phase, nv);
     d.sch32 = nullptr;
     if (r->precision) AL(d.sch32, 60 * nv);
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
@@ -597,6 +612,10 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     CUDA_TRY(cudaMemcpyAsync(d_eul, mesh->euler_deg, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(d.phase, mesh->phase, sizeof(int) * nv, cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMallocHost(&r->h_flag, 64));
+    r->nl = *nl;
+    r->phase.assign(mesh->phase, mesh->phase + nv);
+    if (mesh->grain) r->grain.assign(mesh->grain, mesh->grain + nv);
+    else r->grain.assign(nv, 1);
     long long nph1 = 0;
     for (long long v = 0; v < nv; ++v) nph1 += mesh->phase[v] == 1;
     d.wgt_ph1 = (1.0 * (double)nph1) / Nxyz;
@@ -965,8 +984,8 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out)
     int per;
     switch (field) {
     case 0: case 1: case 2: case 3: case 4: per = 9; break;
-    case 5: case 6: per = 12; break;
-    case 7: case 8: case 9: per = 1; break;
+    case 5: case 6: case 10: case 11: per = 12; break;
+    case 7: case 8: case 9: case 12: case 13: case 14: per = 1; break;
     case 20: case 21: per = 6; break;
     default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
     }
@@ -1042,8 +1061,8 @@ int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out)
     int per;
     switch (field) {
     case 0: case 1: case 2: case 3: case 4: per = 9; break;
-    case 5: case 6: per = 12; break;
-    case 7: case 8: case 9: per = 1; break;
+    case 5: case 6: case 10: case 11: per = 12; break;
+    case 7: case 8: case 9: case 12: case 13: case 14: per = 1; break;
     case 20: case 21: per = 6; break;
     default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
     }
@@ -1061,6 +1080,21 @@ int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out)
     int rc = noalloc_download(r, field, n, dev, host_out);
     if (dev != cur) cudaSetDevice(cur);
     return rc;
+}
+
+int voce_rve_get_ids(const voce_rve *r, int *grain, int *phase)
+{
+    if (!r) return fail(VOCE_ERR_ARG, "null argument");
+    if (grain) std::memcpy(grain, r->grain.data(), sizeof(int) * r->grain.size());
+    if (phase) std::memcpy(phase, r->phase.data(), sizeof(int) * r->phase.size());
+    return VOCE_OK;
+}
+
+int voce_rve_get_namelist(const voce_rve *r, voce_namelist *out)
+{
+    if (!r || !out) return fail(VOCE_ERR_ARG, "null argument");
+    *out = r->nl;
+    return VOCE_OK;
 }
 
 int voce_rve_destroy(voce_rve *r)

@@ -15,6 +15,8 @@
 //   itau[24][nv]  1/crss
 //   gamacum[nv], gtot[12][nv], edot[5][nv], gamdot[12][nv], taux[12][nv],
 //   svm[nv], evm[nv], phase[nv]
+//   diag[3][nv]   post-increment diagnostics rho_rss, rho_crss, work_p
+//                 (evolution.c:509-529)
 //   spec[6][nzh][nx][ny] half spectrum (kz = 0..nz/2), complex, y fastest
 //   aacc[3][nzh][nx][ny] antisymmetric part of the Green update, summed
 //                 over the iterations of the current increment
@@ -93,7 +95,7 @@ struct RveDesc {
     // fields
     double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
     float *sch32;        // float copy of sch (mixed-precision Newton only)
-    double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl;
+    double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;
     const void *twx, *twy, *twz;  // exp(-2 pi i j / L), complex of the spectrum type

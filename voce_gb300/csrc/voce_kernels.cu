@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
         for (int c = 0; c < 5; ++c) d.edot[c * nv + v] = 0.0;
         d.svm[v] = 0.0;
         d.evm[v] = 0.0;
+        for (int c = 0; c < 3; ++c) d.diag[c * nv + v] = 0.0;
         if (!d.solid[ph]) {
             for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = 0.0; d.sigp[c * nv + v] = 0.0; }
             for (int c = 0; c < 9; ++c) d.tm[c * nv + v] = (c % 4 == 0) ? 1.0 : 0.0;
@@ -878,6 +879,15 @@ __device__ void incr_end_unit(const RveDesc &d, int unit, int nunits)
                 e5[c] = e5[c] + ed[c] * dt;
                 d.eps[c * nv + v] = e5[c];
             }
+            // resolved shear stresses for the diagnostics, with the Schmid
+            // tensors of this increment (the reorientation below replaces them)
+            double rss[VOCE_NS];
+            if (hrd)
+                for (int k = 0; k < d.nsys; ++k) {
+                    const double *sc = d.sch + (long long)(5 * k) * nv + v;
+                    rss[k] = sc[0] * s6[0] + sc[nv] * s6[1] + sc[2 * nv] * s6[2] + sc[3 * nv] * s6[3] +
+                             sc[4 * nv] * s6[4];
+                }
             if (upd) {
                 double T[3][3], RL[3][3], Lp[3][3], RS[3][3], Rot[3][3];
                 for (int a = 0; a < 3; ++a)
@@ -913,7 +923,21 @@ __device__ void incr_end_unit(const RveDesc &d, int unit, int nunits)
                     for (int b = 0; b < 3; ++b) d.tm[(3 * a + b) * nv + v] = T[a][b];
                 schmid_from_tm(d, v, T);
             }
-            if (hrd) harden_voxel(d, v, gd);
+            if (hrd) {
+                harden_voxel(d, v, gd);
+                // rho_rss, rho_crss, work_p (evolution.c:509-529)
+                const double ref = 0.35 * 47.565 * 0.256;
+                double rr = 0.0, rc = 0.0, wp = 0.0;
+                for (int k = 0; k < d.nsys; ++k) {
+                    const double a = rss[k] / ref, b = d.crss[(2 * k) * nv + v] / ref;
+                    rr += a * a;
+                    rc += b * b;
+                    wp += fabs(d.gtot[k * nv + v] * rss[k]);
+                }
+                d.diag[v] = rr;
+                d.diag[nv + v] = rc;
+                d.diag[2 * nv + v] = wp;
+            }
         } else {
             for (int c = 0; c < 5; ++c) d.edot[c * nv + v] = 0.0;
         }
@@ -1051,6 +1075,13 @@ __global__ void k_field_out(RveDesc d, int field, double *out)
         case 7: out[v] = d.gamacum[v]; break;
         case 8: out[v] = d.svm[v]; break;
         case 9: out[v] = d.evm[v]; break;
+        case 10:
+            for (int k = 0; k < VOCE_NS; ++k) out[VOCE_NS * v + k] = d.gtot[k * nv + v];
+            break;
+        case 11:
+            for (int k = 0; k < VOCE_NS; ++k) out[VOCE_NS * v + k] = d.taux[k * nv + v];
+            break;
+        case 12: case 13: case 14: out[v] = d.diag[(field - 12) * nv + v]; break;
         case 20: case 21:
             b_to_t6<double>(b6, t6);
             for (int c = 0; c < 6; ++c) out[(long long)c * nv + v] = t6[c];

@@ -182,6 +182,22 @@ def voronoi_mesh(n: int, n_grains: int, seed: int) -> Mesh:
                 np.ones(n ** 3, dtype=np.int32))
 
 
+def voronoi_mesh_box(dims, n_grains: int, seed: int) -> Mesh:
+    """voronoi_mesh on an nx x ny x nz grid: voxel centres ((i+0.5)/nx,
+    (j+0.5)/ny, (k+0.5)/nz) in the periodic unit cube, brute-force labels
+    (ties: lowest id).  For small grids."""
+    nx, ny, nz = dims
+    rng = np.random.Generator(np.random.PCG64(seed))
+    seeds = rng.random((n_grains, 3))
+    eul_g = so3_uniform_bunge(rng, n_grains)
+    axes = [(np.arange(m) + 0.5) / m for m in (nx, ny, nz)]
+    pts = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    d = pts[:, None, :] - seeds[None, :, :]
+    d -= np.round(d)
+    lab = np.argmin((d * d).sum(-1), axis=1).astype(np.int32)
+    return Mesh((nx, ny, nz), eul_g[lab], lab + 1, np.ones(nx * ny * nz, dtype=np.int32))
+
+
 def write_mesh(path: str, mesh: Mesh) -> None:
     nx, ny, nz = mesh.dims
     ii, jj, kk = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1),
