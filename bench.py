@@ -510,6 +510,15 @@ def run_cfg4(args):
     t_run = time.perf_counter() - t0
     value = nv_tot * args.ticks / t_run           # every RVE is active every tick (checked)
     assert left == len(rves), left
+    # per-phase breakdown: a few more ticks driven from the host with every
+    # launch timed (after the timed region)
+    prof_ticks = 5
+    b.set_profiling(True)
+    b.reset_kernel_times()
+    b.run(max_ticks=prof_ticks)
+    kt = b.kernel_times()
+    b.set_profiling(False)
+    kernel_ms = {k: ms / prof_ticks for k, (ms, n) in kt.items() if n}
     # accuracy: first increment of a few RVEs against the plain FP64 path alone
     errs = []
     for i in range(min(8, len(rves))):
@@ -542,6 +551,9 @@ def run_cfg4(args):
                    "voxels": nv_tot, "mesh_generation_s": t_gen, "setup_s": t_setup},
         "plain_fp64_one_at_a_time": {"value": plain, "per_edge": thr},
         "batched_over_plain": value / plain,
+        "kernel_ms_per_tick": kernel_ms,
+        "kernel_timing": "CUDA events around every launch of %d host-driven ticks after the "
+                         "timed ones" % prof_ticks,
         "first_increment_macro_err_vs_plain_fp64": errs,
     }
     print(json.dumps(res), flush=True)

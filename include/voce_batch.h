@@ -42,6 +42,15 @@ long long voce_batch_ticks(const voce_batch *b);
 /* Detaches the RVEs (they are not destroyed) and frees the batch. */
 int voce_batch_destroy(voce_batch *b);
 
+/* Diagnostics.  With profiling on, voce_batch_run drives the ticks from the
+ * host instead of the graph (same kernels, same results) and brackets every
+ * launch with CUDA events; voce_batch_get_kernel_time then gives the summed
+ * milliseconds and the launch count of kernel k (the VOCE_K_* ids of
+ * voce_gpu_diag.h). */
+int voce_batch_set_profiling(voce_batch *b, int on);
+int voce_batch_get_kernel_time(const voce_batch *b, int k, double *ms, long long *launches);
+int voce_batch_reset_kernel_times(voce_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,3 +86,30 @@ def test_tick_budget_resume_and_rejoin(voce_lib):
         r.run(1)                       # one more increment, alone
         _same(_snapshot(r, n + 1), rf)
         r.close()
+
+
+def test_profiled_ticks_equal_graph_ticks(voce_lib):
+    """Profiling drives the ticks from the host with timed launches: same
+    kernels, bit-identical results, and every phase timed."""
+    cases = _cases()[:4]
+    snaps = []
+    for prof in (False, True):
+        rves = [_make(c, capi.PREC_MIXED) for c, _ in cases]
+        with capi.Batch(capi.PREC_MIXED) as b:
+            for r, (c, n) in zip(rves, cases):
+                b.add(r, n)
+            if prof:
+                b.set_profiling(True)
+            while b.run(max_ticks=9):
+                pass
+            kt = b.kernel_times()
+        snaps.append([_snapshot(r, n) for r, (c, n) in zip(rves, cases)])
+        for r in rves:
+            r.close()
+        if prof:
+            for k in ("fft_z_fwd", "fft_x_green", "nr", "finalize_iter", "incr_end"):
+                assert kt[k][1] > 0 and kt[k][0] > 0.0, k
+        else:
+            assert all(n == 0 for _, n in kt.values())
+    for a, b_ in zip(*snaps):
+        _same(a, b_)

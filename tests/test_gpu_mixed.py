@@ -1,0 +1,79 @@
+"""The mixed-precision form (VOCE_PREC_MIXED: single-precision spectrum,
+Green operator and Newton iterations, double-precision residual acceptance,
+hardening, norms and averages) against the reference's own macro curve and
+fields (golden fixtures) and against the FP64 form on the GPU.
+
+Bounds: the macro stress / strain / strain-rate averages of every increment
+within 1e-4 relative (the bound the mixed form is held to); per-voxel stress
+and strain rate within 1e-3 relative, norm-wise; Green-iteration counts
+within 10 % of the reference's."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import golden_io as gio
+import make_golden
+from voce_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+MACRO_TOL = 1e-4
+FIELD_TOL = 1e-3
+CASES = ["vor8_tension", "vor8_psc", "vor8_gas", "vor8_creep", "vor8_noupd", "vor12_mix",
+         "cfg1_16", "cfg2_64"]
+
+
+def _write(case):
+    return case.write(tempfile.mkdtemp(prefix="mixed_"))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_matches_reference_macro_curve(name, voce_lib):
+    if not gio.available(name):
+        pytest.skip("fixture not generated")
+    make, n, _ = make_golden.CASES[name]
+    case = make()
+    fx = gio.load(name)
+    assert case.mesh.digest() == str(fx["digest"])
+    seg = gio.segment(fx, case.update_flag)
+    nv = case.mesh.nvox
+    with capi.Rve.from_files(_write(case), capi.PREC_MIXED) as r:
+        r.run(n)
+        worst = 0.0
+        for k in range(n):
+            inc = r.increment(k)
+            ref = seg["incr"][k]
+            n_ref = len(ref["its"])
+            assert abs(inc["iters"] - n_ref) <= max(2, 0.1 * n_ref), (k, inc["iters"], n_ref)
+            e = gio.rel(np.array(inc["sig_avg"]) * nv, ref["its"][-1]["sig"].ravel())
+            worst = max(worst, e)
+            assert e < MACRO_TOL, (k, e)
+            assert gio.rel(np.array(inc["eps_avg"]) * nv, ref["eps"].ravel()) < MACRO_TOL
+            assert gio.rel(np.array(inc["edot_avg"]) * nv, ref["edot"].ravel()) < MACRO_TOL
+        sig = r.field("sig_voigt").T
+        edot = r.field("edot_voigt").T
+    if "sample_idx" in fx:
+        idx = fx["sample_idx"]
+        sig, edot = sig[idx], edot[idx]
+    assert gio.rel(sig, fx["sig"]) < FIELD_TOL
+    assert gio.rel(edot, fx["edot"]) < FIELD_TOL
+    print(name, "worst macro rel", worst)
+
+
+def test_mixed_vs_fp64_random_load(voce_lib):
+    rng = np.random.Generator(np.random.PCG64(77))
+    case = synth.small_case(24, 30, 77, n_steps=3, load=synth.random_traceless_load(rng))
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        with capi.Rve.from_files(_write(case), prec) as r:
+            r.run(3)
+            out[prec] = ([r.increment(k) for k in range(3)], r.field("sig_voigt"),
+                         r.field("edot_voigt"), r.field("crss"))
+    (i64, s64, e64, c64), (i32, s32, e32, c32) = out[capi.PREC_FP64], out[capi.PREC_MIXED]
+    for a, b in zip(i32, i64):
+        assert gio.rel(np.array(a["sig_avg"]), np.array(b["sig_avg"])) < MACRO_TOL
+        assert abs(a["iters"] - b["iters"]) <= max(2, 0.1 * b["iters"])
+    assert gio.rel(s32, s64) < FIELD_TOL
+    assert gio.rel(e32, e64) < FIELD_TOL
+    assert gio.rel(c32, c64) < FIELD_TOL

@@ -143,6 +143,10 @@ PROTOTYPES = [
     ("voce_server_result", C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     ("voce_server_bytes_in_use", C.c_longlong, [C.c_void_p]),
     ("voce_server_destroy", C.c_int, [C.c_void_p]),
+    ("voce_batch_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
+    ("voce_batch_get_kernel_time", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_longlong)]),
+    ("voce_batch_reset_kernel_times", C.c_int, [C.c_void_p]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -413,6 +417,23 @@ class Batch:
     @property
     def ticks(self) -> int:
         return int(load().voce_batch_ticks(self._h))
+
+    def set_profiling(self, on: bool) -> None:
+        """Host-driven ticks with every launch timed (same results)."""
+        _check(load().voce_batch_set_profiling(self._h, int(on)))
+
+    def kernel_times(self) -> dict:
+        """{kernel name: (milliseconds, launches)} since the last reset."""
+        out = {}
+        for k, name in enumerate(KERNELS):
+            ms = C.c_double()
+            n = C.c_longlong()
+            _check(load().voce_batch_get_kernel_time(self._h, k, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def reset_kernel_times(self) -> None:
+        _check(load().voce_batch_reset_kernel_times(self._h))
 
     def close(self) -> None:
         if self._h:

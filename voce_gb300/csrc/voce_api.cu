@@ -416,7 +416,7 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
-    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 240 : 0)) + nspec * 9 * cplx;
+    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 420 : 0)) + nspec * 9 * cplx;
 }
 
 // ---------------------------------------------------------------------------
@@ -503,6 +503,9 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         d.gam0[s] = sx.gamd0;
         d.nrs[s] = nr;
         d.g0n[s] = sx.gamd0 * nr;
+        d.gam0f[s] = (float)sx.gamd0;
+        d.nrsf[s] = (float)nr;
+        d.gam0_uniform = 1;   // one slip mode per phase: one gam0
         d.tau0[s] = sx.tau0f;
         d.tau0b[s] = sx.tau0b;
         d.tau1[s] = tau1;
@@ -567,12 +570,14 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
 
     // device memory
     CUDA_TRY(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
-    // Newton / increment-end work split: at most two 128-thread units per SM
-    // (the Newton kernel's registers allow two resident blocks per SM); the
+    // Newton / increment-end work split into 128-thread units: at most one
+    // per Newton block the GPU holds at once (at least two per SM).  The
     // per-RVE partial sums follow this split, so it is fixed per grid size
+    // and precision.
     const long long sm_count = 152;
     long long nb = (nv + 127) / 128;
-    r->npart = (int)(nb < sm_count * 2 ? nb : sm_count * 2);
+    const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(r->precision != 0));
+    r->npart = (int)(nb < cap ? nb : cap);
     d.npart = r->npart;
     int rc = VOCE_OK;
 #define AL(ptr, n) if ((rc = dalloc(r, ptr, (size_t)(n))) != VOCE_OK) { delete r; return rc; }
@@ -581,7 +586,9 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
     AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.diag, 3 * nv); AL(d.phase, nv);
     d.sch32 = nullptr;
-    if (r->precision) AL(d.sch32, 60 * nv);
+    d.itau32 = nullptr;
+    d.sgp32 = nullptr;
+    if (r->precision) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
     AL(d.macro, 1);
     d.incr_cap = 32;   // increments per host read-back
@@ -636,6 +643,8 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     std::memcpy(S066, C066, sizeof(S066));
     if (!lu_inv66(S066)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066"); }
     std::memcpy(d.S0, S066, sizeof(S066));
+    for (int q = 0; q < 36; ++q) d.S0f[q] = (float)d.S0[q];
+    if (r->precision) CUDA_TRY(launch_fill_p32(d, r->stream));
     double C0t[81];
     c66_to_t4(&C066[0][0], C0t);
     c66_to_t4(&S066[0][0], d.S0t);
@@ -1208,6 +1217,7 @@ struct voce_batch {
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
     long long ticks_total = 0;
+    Prof prof;
     void drop_graph()
     {
         if (exec) cudaGraphExecDestroy(exec);
@@ -1229,6 +1239,8 @@ struct voce_batch {
         drop_plan();
         if (d_ctl) cudaFree(d_ctl);
         if (h_ctl) cudaFreeHost(h_ctl);
+        for (int k = 0; k < 2 * K_COUNT; ++k)
+            if (prof.ev[k]) cudaEventDestroy(prof.ev[k]);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1357,9 +1369,21 @@ int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
     b->h_ctl[1] = max_ticks;
     b->h_ctl[2] = 0;
     CUDA_TRY(cudaMemcpyAsync(b->d_ctl, b->h_ctl, 3 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
-    CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
-    CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    if (b->prof.on) {
+        // host-driven ticks with every launch timed; stops where the graph's
+        // WHILE condition would
+        for (int t = 0; t < max_ticks; ++t) {
+            CUDA_TRY(launch_batch_tick_timed(b->plan, b->stream, b->prof));
+            CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+            CUDA_TRY(cudaStreamSynchronize(b->stream));
+            b->prof.collect();
+            if (b->h_ctl[2] == 0) break;
+        }
+    } else {
+        CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
+        CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        CUDA_TRY(cudaStreamSynchronize(b->stream));
+    }
     CUDA_TRY(cudaGetLastError());
     b->ticks_total += b->h_ctl[0];
     for (voce_rve *r : b->rves) {
@@ -1372,6 +1396,33 @@ int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
 }
 
 long long voce_batch_ticks(const voce_batch *b) { return b ? b->ticks_total : -1; }
+
+int voce_batch_set_profiling(voce_batch *b, int on)
+{
+    if (!b) return fail(VOCE_ERR_ARG, "null argument");
+    if (on && !b->prof.ev[0])
+        for (int k = 0; k < 2 * K_COUNT; ++k) CUDA_TRY(cudaEventCreate(&b->prof.ev[k]));
+    b->prof.on = on != 0;
+    return VOCE_OK;
+}
+
+int voce_batch_get_kernel_time(const voce_batch *b, int k, double *ms, long long *launches)
+{
+    if (!b || k < 0 || k >= K_COUNT) return fail(VOCE_ERR_ARG, "bad argument");
+    if (ms) *ms = b->prof.ms[k];
+    if (launches) *launches = b->prof.n[k];
+    return VOCE_OK;
+}
+
+int voce_batch_reset_kernel_times(voce_batch *b)
+{
+    if (!b) return fail(VOCE_ERR_ARG, "null argument");
+    for (int k = 0; k < K_COUNT; ++k) {
+        b->prof.ms[k] = 0.0;
+        b->prof.n[k] = 0;
+    }
+    return VOCE_OK;
+}
 
 int voce_batch_destroy(voce_batch *b)
 {

@@ -28,6 +28,10 @@
 #define VOCE_NPART 16
 #define VOCE_MAXRAD 12
 #define VOCE_ITLOG 12   // doubles per logged iteration
+// Mixed form: Green iterations whose predecessor's normalised error is above
+// this (and the first of every increment) run the Newton solve in single
+// precision only; the rest end it on the double-precision residual.
+#define VOCE_POLISH_ERR 1e-3
 
 // Lebensohn-Tome basis constants, the literal values of kinematics.c:333-335
 #define RSQ2 0.70710678118654744
@@ -77,10 +81,13 @@ struct RveDesc {
     int mixed;           // spectrum precision: 0 double, 1 float
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
+    float gam0f[VOCE_NS], nrsf[VOCE_NS];   // float copies for the mixed Newton
+    int gam0_uniform;    // every system has the same gam0
     double tau0[VOCE_NS], tau1[VOCE_NS], thet0[VOCE_NS], thet1[VOCE_NS];
     double hard[VOCE_NS * VOCE_NS];
     double bn[VOCE_NS * 3], bb[VOCE_NS * 3];
     double S0[36];       // S066 (B basis)
+    float S0f[36];       // float copy (mixed-precision error norms)
     double S0t[81];      // S0 as 3x3x3x3 (get_smacro's dDisGradAvg)
     double Kq[36];       // acoustic tensor coefficients: K6 = Kq * nn6
     double Udot[9], Scauchy[9];
@@ -95,6 +102,8 @@ struct RveDesc {
     // fields
     double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
     float *sch32;        // float copy of sch (mixed-precision Newton only)
+    float *itau32;       // float copy of itau (mixed-precision Newton only)
+    float *sgp32;        // float (S_g + S0), packed upper triangle (mixed-precision Newton only)
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;
@@ -273,6 +282,61 @@ __device__ __forceinline__ void flow_rule(const RveDesc &d, long long v, const d
                 for (int j = i; j < 5; ++j) { D[q] = fma(t[i], scd[j], D[q]); ++q; }
         }
     }
+}
+
+// |a|^e in single precision: the same product chain as pow_abs_e.
+__device__ __forceinline__ float pow_abs_ef(float a, int e)
+{
+    if (e == 19) {
+        const float a2 = a * a, a4 = a2 * a2, a8 = a4 * a4, a16 = a8 * a8;
+        return (a16 * a2) * a;
+    }
+    float res = 1.0f, b = a;
+    while (e) {
+        if (e & 1) res *= b;
+        b *= b;
+        e >>= 1;
+    }
+    return res;
+}
+
+// flow_rule entirely in single precision (mixed-precision Newton, integer
+// exponent only): strain rate and its 5x5 Jacobian (packed upper triangle)
+// at the stress s.  Returns false when a resolved-shear ratio is too large
+// for |r|^n in single precision, or not finite.
+__device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, long long v, const float *s,
+                                              float *edot, float *D)
+{
+    const long long nv = d.nv;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) edot[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 15; ++i) D[i] = 0.0f;
+    for (int k = 0; k < d.nsys; ++k) {
+        float sc[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch32 + (long long)(5 * k + i) * nv + v);
+        const float rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const int neg = rss < 0.0f;
+        const float it = __ldg(d.itau32 + (long long)(2 * k + neg) * nv + v);
+        const float r = rss * it;
+        const float ar = fabsf(r);
+        if (!(ar < 60.0f)) return false;
+        const float q = d.gam0f[k] * pow_abs_ef(ar, d.ipow_n - 1);
+        const float g2 = q * r, g1 = (q * it) * d.nrsf[k];
+        float t[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            edot[i] = fmaf(sc[i], g2, edot[i]);
+            t[i] = g1 * sc[i];
+        }
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+#pragma unroll
+            for (int j = i; j < 5; ++j) { D[c] = fmaf(t[i], sc[j], D[c]); ++c; }
+    }
+    return true;
 }
 
 // Solve M x = b for symmetric positive definite M (6x6, full storage, only

@@ -179,6 +179,8 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             if (d.sch32)
                 for (int c = 0; c < 60; ++c) d.sch32[c * nv + v] = 0.0f;
             for (int c = 0; c < 24; ++c) { d.crss[c * nv + v] = 0.0; d.itau[c * nv + v] = 0.0; }
+            if (d.itau32)
+                for (int c = 0; c < 24; ++c) d.itau32[c * nv + v] = 0.0f;
             continue;
         }
         acc[0] += 1.0;
@@ -222,6 +224,10 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             d.crss[(2 * k + 1) * nv + v] = d.tau0b[k];
             d.itau[(2 * k) * nv + v] = 1.0 / d.tau0[k];
             d.itau[(2 * k + 1) * nv + v] = 1.0 / d.tau0b[k];
+            if (d.itau32) {
+                d.itau32[(2 * k) * nv + v] = (float)(1.0 / d.tau0[k]);
+                d.itau32[(2 * k + 1) * nv + v] = (float)(1.0 / d.tau0b[k]);
+            }
         }
         double T[3][3];
         for (int i = 0; i < 3; ++i)
@@ -465,18 +471,265 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
 // solved in the equivalent symmetric form
 //   (S0 + S_g + dt dEdot) dsig = S0 R
 // where R is the reference's residual (evolution.c:78-83) and S0 = C0^-1.
-// MIXED_NR: the residual, the update and the stop test stay in FP64; the
-// Jacobian and its LDL^T solve run in FP32 (an inexact Newton step that
-// converges to the same FP64 fixed point).
+// MIXED_NR: see mixed_newton below.
 // ---------------------------------------------------------------------------
+
+// P = S_g + S0 (packed upper triangle) of voxel v
+__device__ __forceinline__ void load_P(const RveDesc &d, long long v, double (&P)[21])
+{
+#pragma unroll
+    for (int q = 0; q < 21; ++q) P[q] = __ldg(d.sg + (long long)q * d.nv + v);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) P[sym6(i, j)] += d.S0[i * 6 + j];
+}
+
+// The same, with loads the compiler may not merge with earlier ones: a
+// reload where keeping P live would cost registers.
+__device__ __forceinline__ void reload_P(const RveDesc &d, long long v, double (&P)[21])
+{
+#pragma unroll
+    for (int q = 0; q < 21; ++q) {
+        const double *a = d.sg + (long long)q * d.nv + v;
+        double x;
+        asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(x) : "l"(a));
+        P[q] = x;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) P[sym6(i, j)] += d.S0[i * 6 + j];
+}
+
+// Newton steps on the FP64 residual with an FP32 Jacobian and solve (an
+// inexact Newton step converging to the same FP64 fixed point); the loop of
+// the FP64 form with the stop test of evolution.c:112.
+template <bool MIXED_NR>
+__device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const double (&P)[21],
+                                           const double (&cc)[6], double thr, double (&sig)[6],
+                                           double (&sp)[6], double (&Rl)[6], int &it)
+{
+    const double dt = d.dt;
+    bool go = true;
+    while (go && it < 100) {
+        ++it;
+        double ed[5];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sp[c] = sig[c];
+        double R[6];
+        if (MIXED_NR) {
+            float D[15];
+            flow_rule<true, false, float>(d, v, sig, ed, D, nullptr, nullptr);
+            float M[6][6], x[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+                R[i] = s;
+                Rl[i] = s;
+                x[i] = (float)s;
+            }
+            const float dtf = (float)dt;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = 0; j <= i; ++j) {
+                    float m = (float)P[sym6(i, j)];
+                    if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    M[i][j] = m;
+                }
+            ldlt_solve6f(M, x);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
+        } else {
+            double D[15];
+            flow_rule<true, false, double>(d, v, sig, ed, D, nullptr, nullptr);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+                R[i] = s;
+                Rl[i] = s;
+            }
+            double M[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = 0; j <= i; ++j) {
+                    double m = P[sym6(i, j)];
+                    if (i < 5 && j < 5) m = fma(dt, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    M[i][j] = m;
+                }
+            ldlt_solve6(M, R);
+        }
+        double cnr = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double sn = sig[c] - R[c];
+            const double dd = sn - sig[c];
+            cnr = fma(dd, dd, cnr);
+            sig[c] = sn;
+        }
+        go = cnr > thr;
+    }
+}
+
+// Strain rate only, in double precision, for the mixed form's residual: the
+// flow rule with |r|^n sign(r) formed as copysign(r^n, r) (n = 20: r^20 by
+// four squarings and one product) and gam0 taken out of the sum when all
+// systems share it.
+__device__ __forceinline__ void edot_fp64(const RveDesc &d, long long v, const double *s, double *edot)
+{
+    const long long nv = d.nv;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) edot[i] = 0.0;
+    const bool n20 = d.ipow_n == 20, uni = d.gam0_uniform != 0;
+    for (int k = 0; k < d.nsys; ++k) {
+        double sc[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
+        const double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const int neg = rss < 0.0;
+        const double r = rss * __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
+        double g;
+        if (n20) {
+            const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8;
+            g = copysign(r16 * r4, r);
+        } else {
+            g = pow_abs_e(fabs(r), d.ipow_n - 1) * r;
+        }
+        if (!uni) g *= d.gam0[k];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) edot[i] = fma(sc[i], g, edot[i]);
+    }
+    if (uni) {
+#pragma unroll
+        for (int i = 0; i < 5; ++i) edot[i] *= d.gam0[0];
+    }
+}
+
+// Mixed form: Newton in single precision (residual, Jacobian and solve) down
+// to a relative update of 1e-4, then one Newton step on the double-precision
+// residual with the last single-precision matrix.  That step is accepted when
+// its relative update is below 1e-5: Newton's quadratic term then puts the
+// next update near 1e-9, under the 1e-7 test of the FP64 form, so the
+// accepted stress is taken as the converged point (zero residual, and the
+// point the strain rate is later evaluated at).  Anything else continues with
+// newton_fp64 from where it stands.
+__device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, const double (&lam)[6],
+                                             const double (&cc)[6], double sn2, bool polish,
+                                             double (&sig)[6], double (&sp)[6], double (&Rl)[6],
+                                             int &it)
+{
+    const double dt = d.dt;
+    bool done = false;
+    if (d.ipow_n >= 1) {
+        float sf[6], Mf[6][6], Pf[21];
+#pragma unroll
+        for (int q = 0; q < 21; ++q) Pf[q] = __ldg(d.sgp32 + (long long)q * d.nv + v);
+        float ccf[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { sf[c] = (float)lam[c]; ccf[c] = (float)cc[c]; }
+        // single precision alone stops at a relative update of 1e-5, before a
+        // polish step at 1e-4
+        const float thr32 = (float)((polish ? 1e-8 : 1e-10) * sn2);
+        const float dtf = (float)dt;
+        bool ok = true, conv = false;
+        while (it < 24) {
+            ++it;
+            float ed[5], D[15], x[6];
+            if (!flow_rule_f32(d, v, sf, ed, D)) { ok = false; break; }
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                float t = ccf[i] + (i < 5 ? dtf * ed[i] : 0.0f);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) t = fmaf(Pf[sym6(i, j)], sf[j], t);
+                x[i] = t;
+            }
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = 0; j <= i; ++j) {
+                    float m = Pf[sym6(i, j)];
+                    if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    Mf[i][j] = m;
+                }
+            ldlt_solve6f(Mf, x);
+            float dn = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) { dn = fmaf(x[c], x[c], dn); sf[c] -= x[c]; }
+            if (!(dn <= 3.0e38f)) { ok = false; break; }   // not finite
+            if (dn < thr32) { conv = true; break; }
+        }
+        if (ok && conv && !polish) {
+            done = true;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) { sig[c] = (double)sf[c]; sp[c] = sig[c]; Rl[c] = 0.0; }
+        } else if (ok && conv) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c];
+            ++it;
+            double ed[5];
+            edot_fp64(d, v, sig, ed);
+            double P[21];
+            reload_P(d, v, P);
+            float x[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                double t = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) t = fma(P[sym6(i, j)], sig[j], t);
+                Rl[i] = t;
+                x[i] = (float)t;
+            }
+            ldlt_solve6f(Mf, x);
+            double cnr = 0.0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const double sn = sig[c] - (double)x[c];
+                const double dd = sn - sig[c];
+                cnr = fma(dd, dd, cnr);
+                sig[c] = sn;
+            }
+            if (cnr <= 1e-10 * sn2) {
+                done = true;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) { sp[c] = sig[c]; Rl[c] = 0.0; }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) sp[c] = (double)sf[c];
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sig[c] = lam[c];
+        }
+    }
+    if (!done) {
+        double P[21];
+        reload_P(d, v, P);
+        newton_fp64<true>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+    }
+}
+
 template <bool MIXED_NR>
 __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 {
-    double acc[VOCE_NPART];
+    // per-thread sums in shared memory (one slot per thread, the same
+    // additions in the same order as register accumulators) keep them out of
+    // the registers the Newton loop needs
+    __shared__ double s_acc[VOCE_NPART][128];
+    const int tid = threadIdx.x;
+    bool polish = true;
+    if (MIXED_NR) {
+        const MacroDev *m = d.macro;
+        polish = !m->first_iter && fmax(fabs(m->Err_e), fabs(m->Err_s)) <= VOCE_POLISH_ERR;
+    }
 #pragma unroll
-    for (int q = 0; q < VOCE_NPART; ++q) acc[q] = 0.0;
+    for (int q = 0; q < VOCE_NPART; ++q) s_acc[q][tid] = 0.0;
     const long long nv = d.nv;
-    const double dt = d.dt;
     for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
          v += (long long)nunits * blockDim.x) {
         const int ph = d.phase[v];
@@ -485,130 +738,90 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = 0.0; d.sigp[c * nv + v] = 0.0; }
             continue;
         }
-        double lam[6], e6[6], ep[6], P[21];
+        double lam[6], cc[6];
+        {
+            double e6[6], ep[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            lam[c] = d.sig[c * nv + v];
-            e6[c] = d.dgs[c * nv + v];
-        }
+            for (int c = 0; c < 6; ++c) {
+                lam[c] = d.sig[c * nv + v];
+                e6[c] = d.dgs[c * nv + v];
+            }
 #pragma unroll
-        for (int c = 0; c < 5; ++c) ep[c] = d.eps[c * nv + v];
-        ep[5] = 0.0;
+            for (int c = 0; c < 5; ++c) ep[c] = d.eps[c * nv + v];
+            ep[5] = 0.0;
 #pragma unroll
-        for (int q = 0; q < 21; ++q) P[q] = __ldg(d.sg + (long long)q * nv + v);
-        double cc[6];
+            for (int i = 0; i < 6; ++i) {
+                double s = ep[i] - e6[i];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            double s = ep[i] - e6[i];
-#pragma unroll
-            for (int j = 0; j < 6; ++j) s = fma(-d.S0[i * 6 + j], lam[j], s);
-            cc[i] = s;
-        }
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int j = i; j < 6; ++j) P[sym6(i, j)] += d.S0[i * 6 + j];
-        float Pf[21];
-        if (MIXED_NR) {
-#pragma unroll
-            for (int q = 0; q < 21; ++q) Pf[q] = (float)P[q];
+                for (int j = 0; j < 6; ++j) s = fma(-d.S0[i * 6 + j], lam[j], s);
+                cc[i] = s;
+            }
         }
         double sn2 = 0.0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) sn2 = fma(lam[c], lam[c], sn2);
-        // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
-        const double thr = 1e-14 * sn2;
         double sig[6], sp[6], Rl[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) { sig[c] = lam[c]; sp[c] = lam[c]; Rl[c] = 0.0; }
         int it = 0;
-        bool go = true;
-        while (go && it < 100) {
-            ++it;
-            double ed[5];
-#pragma unroll
-            for (int c = 0; c < 6; ++c) sp[c] = sig[c];
-            double R[6];
-            if (MIXED_NR) {
-                float D[15];
-                flow_rule<true, false, float>(d, v, sig, ed, D, nullptr, nullptr);
-                float M[6][6], x[6];
-#pragma unroll
-                for (int i = 0; i < 6; ++i) {
-                    double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
-#pragma unroll
-                    for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
-                    R[i] = s;
-                    Rl[i] = s;
-                    x[i] = (float)s;
-                }
-                const float dtf = (float)dt;
-#pragma unroll
-                for (int i = 0; i < 6; ++i)
-#pragma unroll
-                    for (int j = 0; j <= i; ++j) {
-                        float m = Pf[sym6(i, j)];
-                        if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
-                        M[i][j] = m;
-                    }
-                ldlt_solve6f(M, x);
-#pragma unroll
-                for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
-            } else {
-                double D[15];
-                flow_rule<true, false, double>(d, v, sig, ed, D, nullptr, nullptr);
-#pragma unroll
-                for (int i = 0; i < 6; ++i) {
-                    double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
-#pragma unroll
-                    for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
-                    R[i] = s;
-                    Rl[i] = s;
-                }
-                double M[6][6];
-#pragma unroll
-                for (int i = 0; i < 6; ++i)
-#pragma unroll
-                    for (int j = 0; j <= i; ++j) {
-                        double m = P[sym6(i, j)];
-                        if (i < 5 && j < 5) m = fma(dt, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
-                        M[i][j] = m;
-                    }
-                ldlt_solve6(M, R);
-            }
-            double cnr = 0.0;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const double sn = sig[c] - R[c];
-                const double dd = sn - sig[c];
-                cnr = fma(dd, dd, cnr);
-                sig[c] = sn;
-            }
-            go = cnr > thr;
+        if (MIXED_NR) {
+            mixed_newton(d, v, lam, cc, sn2, polish, sig, sp, Rl, it);
+        } else {
+            double P[21];
+            load_P(d, v, P);
+            // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
+            newton_fp64<false>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
         }
-        double cs = 0.0, ce = 0.0;
+        double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
+        if (MIXED_NR) {
+            // error norms in single precision: they only steer the Green
+            // iteration's stop test at 1e-5
+            float ds[6], dp[6], cs = 0.0f, ce = 0.0f;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            const double ds = sig[i] - lam[i];
-            cs = fma(ds, ds, cs);
-            double te = Rl[i];
+            for (int i = 0; i < 6; ++i) {
+                ds[i] = (float)(sig[i] - lam[i]);
+                dp[i] = (float)(sp[i] - lam[i]);
+                cs = fmaf(ds[i], ds[i], cs);
+            }
 #pragma unroll
-            for (int j = 0; j < 6; ++j) te = fma(-d.S0[i * 6 + j], sp[j] - lam[j], te);
-            ce = fma(te, te, ce);
+            for (int i = 0; i < 6; ++i) {
+                float te = (float)Rl[i];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) te = fmaf(-d.S0f[i * 6 + j], dp[j], te);
+                ce = fmaf(te, te, ce);
+            }
+            ncs = (double)sqrtf(cs);
+            nce = (double)sqrtf(ce);
+        } else {
+            double cs = 0.0, ce = 0.0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                const double ds = sig[i] - lam[i];
+                cs = fma(ds, ds, cs);
+                double te = Rl[i];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) te = fma(-d.S0[i * 6 + j], sp[j] - lam[j], te);
+                ce = fma(te, te, ce);
+            }
+            ncs = sqrt(cs);
+            nce = sqrt(ce);
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = sig[c]; d.sigp[c * nv + v] = sp[c]; }
-        acc[0] += sqrt(cs);
-        acc[1] += sqrt(ce);
+        s_acc[0][tid] += ncs;
+        s_acc[1][tid] += nce;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) acc[2 + c] += sig[c];
+        for (int c = 0; c < 6; ++c) s_acc[2 + c][tid] += sig[c];
         if (ph == 1) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) acc[8 + c] += sig[c];
+            for (int c = 0; c < 6; ++c) s_acc[8 + c][tid] += sig[c];
         }
-        acc[14] += (double)it;
-        acc[15] = fmax(acc[15], (double)it);
+        s_acc[14][tid] += (double)it;
+        s_acc[15][tid] = fmax(s_acc[15][tid], (double)it);
     }
+    double acc[VOCE_NPART];
+#pragma unroll
+    for (int q = 0; q < VOCE_NPART; ++q) acc[q] = s_acc[q][tid];
     block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
 
@@ -657,6 +870,10 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
     if (threadIdx.x != 0) return;
     MacroDev *m = d.macro;
     static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
+    // the mixed form's Newton ran in single precision alone this iteration
+    // (the predicate nr_unit used): it may not end the increment
+    const bool fp32_only =
+        d.mixed && (m->first_iter || fmax(fabs(m->Err_e), fabs(m->Err_s)) > VOCE_POLISH_ERR);
     double Err_e = tot[1] * d.wgt, Err_s = tot[0] * d.wgt;
     double s9[9], s19[9];
     sym9_from_b(tot + 2, s9);
@@ -704,7 +921,8 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
     t6_to_b<double>(t6, m->ddg6);
     m->first_iter = 0;
     m->pending_prelude = 0;
-    const bool more = (m->iter < d.iter_max) && (fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
+    const bool more = (m->iter < d.iter_max) &&
+                      (fp32_only || fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
     m->converged = more ? 0 : 1;
     if (!more) {
         // epilogue macro bookkeeping (evolution.c:438-461)
@@ -769,6 +987,10 @@ __device__ void harden_voxel(const RveDesc &d, long long v, const double *gd)
         d.crss[(2 * i + 1) * nv + v] = c1;
         d.itau[(2 * i) * nv + v] = 1.0 / c0;
         d.itau[(2 * i + 1) * nv + v] = 1.0 / c1;
+        if (d.itau32) {
+            d.itau32[(2 * i) * nv + v] = (float)(1.0 / c0);
+            d.itau32[(2 * i + 1) * nv + v] = (float)(1.0 / c1);
+        }
     }
     d.gamacum[v] = gamtot + deltgam;
 }
@@ -1172,8 +1394,15 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
     }
 }
 
+// resident blocks of 128 threads per SM the mixed Newton kernel is compiled
+// for (register budget 65536 / (128 x blocks))
+#ifndef VOCE_NR_MIXED_BLOCKS
+#define VOCE_NR_MIXED_BLOCKS 3
+#endif
+
 template <bool MIXED_NR>
-__global__ void __launch_bounds__(128) kb_nr(const RveDesc *descs, const int2 *map, int total)
+__global__ void __launch_bounds__(128, MIXED_NR ? VOCE_NR_MIXED_BLOCKS : 1)
+kb_nr(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
@@ -1222,7 +1451,7 @@ __global__ void __launch_bounds__(256) kb_finalize(const RveDesc *descs, int nrv
 // loop condition of the batch: continue while any RVE is active and the
 // tick budget is not spent
 __global__ void kb_cond(const RveDesc *descs, int nrve, int *ticks, const int *max_ticks,
-                        int *active_out, cudaGraphConditionalHandle cond)
+                        int *active_out, cudaGraphConditionalHandle cond, int use_cond)
 {
     __shared__ int any;
     if (threadIdx.x == 0) any = 0;
@@ -1235,7 +1464,7 @@ __global__ void kb_cond(const RveDesc *descs, int nrve, int *ticks, const int *m
         const int t = *ticks + 1;
         *ticks = t;
         *active_out = any;
-        cudaGraphSetConditional(cond, (any > 0 && t < *max_ticks) ? 1u : 0u);
+        if (use_cond) cudaGraphSetConditional(cond, (any > 0 && t < *max_ticks) ? 1u : 0u);
     }
 }
 
@@ -1322,6 +1551,23 @@ cudaError_t set_batch_smem(const BatchPlan &bp)
     return bp.mixed ? set_batch_smem_t<float>(bp) : set_batch_smem_t<double>(bp);
 }
 
+// Newton-kernel blocks resident per GPU (SMs x blocks per SM): the grid cap
+// of kb_nr and the most units an RVE is split into for it
+int nr_resident_blocks(bool mixed)
+{
+    static int cached[2] = {0, 0};
+    int &c = cached[mixed ? 1 : 0];
+    if (!c) {
+        int dev = 0, sms = 152, per = 2;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, 128, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, 128, 0);
+        c = sms * (per > 0 ? per : 1);
+    }
+    return c;
+}
+
 static int grid_for(int total, int cap)
 {
     return total < cap ? (total > 0 ? total : 1) : cap;
@@ -1358,8 +1604,12 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
     pf.end(K_FFT_Z_INV, s);
     pf.begin(K_NR, s);
-    if (bp.mixed) kb_nr<true><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
-    else kb_nr<false><<<grid_for(bp.total[BP_NP], NG), 128, 0, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
+    if (bp.mixed)
+        kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), 128, 0, s>>>(
+            D, bp.map[BP_NP], bp.total[BP_NP]);
+    else
+        kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), 128, 0, s>>>(
+            D, bp.map[BP_NP], bp.total[BP_NP]);
     pf.end(K_NR, s);
     pf.begin(K_FIN_ITER, s);
     kb_finalize<<<grid_for(bp.nrve, 152 * 4), 256, 0, s>>>(D, bp.nrve, 0, cond, use_cond);
@@ -1412,7 +1662,37 @@ cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphCond
     launch_plan_prelude(bp, s, none);
     launch_plan_iteration(bp, s, none, 0, 0);
     launch_plan_incr_end(bp, s, none);
-    kb_cond<<<1, 256, 0, s>>>(bp.descs, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, cond);
+    kb_cond<<<1, 256, 0, s>>>(bp.descs, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, cond, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_tick_timed(const BatchPlan &bp, cudaStream_t s, Prof &pf)
+{
+    launch_plan_prelude(bp, s, pf);
+    launch_plan_iteration(bp, s, pf, 0, 0);
+    launch_plan_incr_end(bp, s, pf);
+    kb_cond<<<1, 256, 0, s>>>(bp.descs, bp.nrve, bp.ticks, bp.max_ticks, bp.active_out, 0, 0);
+    pf.launches += 1;
+    return cudaGetLastError();
+}
+
+// sgp32 = (float)(S_g + S0) once S0 is known (mixed form)
+__global__ void k_fill_p32(RveDesc d)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < d.nv;
+         v += (long long)gridDim.x * blockDim.x) {
+        double P[21];
+        load_P(d, v, P);
+        const bool solid = d.solid[d.phase[v]] != 0;
+        for (int q = 0; q < 21; ++q) d.sgp32[(long long)q * d.nv + v] = solid ? (float)P[q] : 0.0f;
+    }
+}
+
+cudaError_t launch_fill_p32(const RveDesc &d, cudaStream_t s)
+{
+    int blocks = (int)((d.nv + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_fill_p32<<<blocks, 256, 0, s>>>(d);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,8 @@ cudaError_t set_batch_smem(const BatchPlan &bp);
 // one tick: prelude (pending), one Green iteration of every active RVE, the
 // increment end of every RVE that converged, the loop condition
 cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond);
+// the same tick outside a graph, every launch bracketed by pf's events
+cudaError_t launch_batch_tick_timed(const BatchPlan &bp, cudaStream_t s, Prof &pf);
 // The phases of a plan (a lone RVE runs as a plan of one, with the same
 // kernels as any batch): prelude; one Green iteration, whose finaliser sets
 // the WHILE condition when use_cond; the increment end.
@@ -79,6 +81,10 @@ cudaError_t launch_plan_iteration(const BatchPlan &bp, cudaStream_t s, Prof &pf,
                                   cudaGraphConditionalHandle cond, int use_cond);
 cudaError_t launch_plan_incr_end(const BatchPlan &bp, cudaStream_t s, Prof &pf);
 cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
+// the mixed form's float (S_g + S0), once S0 is set in d
+cudaError_t launch_fill_p32(const RveDesc &d, cudaStream_t s);
+// kb_nr blocks resident on the current GPU (SMs x blocks per SM)
+int nr_resident_blocks(bool mixed);
 double measure_fp64_tflops();
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s);
