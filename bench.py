@@ -8,7 +8,10 @@ Green-operator fixed-point iterations until the error norms reach Err = 1e-5
 = sum over steps of (voxels x Green iterations) / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl voce|reference]
-                  [--precision fp64|mixed]
+                  [--precision fp64|mixed|mixed_nr32] [--config cfg2|cfg3|cfg4|cfg5]
+
+--config cfg3 (256^3 mixed forms vs FP64), cfg4 (batched RVEs), cfg5
+(served requests) are the other workloads' modes; they report every form.
 
 --impl reference times the CPU implementation of the same step (the oracle's
 C restatement of the reference, all host threads) on bounded samples.
@@ -34,13 +37,34 @@ ITER_BYTES_PER_VOXEL = 816   # algorithmic bytes per voxel-iteration (plain FP64
 FLUSH_BYTES = 512 << 20      # > 129 MB L2
 
 
+def _prec(name):
+    from voce_gb300 import capi
+    return {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED,
+            "mixed_nr32": capi.PREC_MIXED_NR32}[name]
+
+
+PREC = {k: (lambda k=k: _prec(k)) for k in ("fp64", "mixed", "mixed_nr32")}
+# the arithmetic types each form computes in
+DTYPE = {"fp64": "f64", "mixed": "f32 spectrum+f64 newton",
+         "mixed_nr32": "f32 spectrum+f32 newton+f64 acceptance"}
+FORM_DOC = {"mixed": "FP32 spectrum and Green operator; FP64 Newton, hardening, norms, averages",
+            "mixed_nr32": "as mixed, with FP32 Newton iterations ended by an FP64-residual "
+                          "acceptance step (FP32-only while the Green error is above 1e-3) "
+                          "and FP32 per-voxel error norms"}
+
+
+def _other_mixed(name):
+    return "mixed" if name == "mixed_nr32" else "mixed_nr32"
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="voce", choices=["voce", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default=None, choices=["fp64", "mixed", "mixed_nr32"],
+                   help="default: fp64 (cfg2), mixed_nr32 (cfg3, cfg4, cfg5)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--rves", type=int, default=512, help="cfg4: RVEs in the batch")
     p.add_argument("--ticks", type=int, default=120, help="cfg4: timed batch ticks")
@@ -250,7 +274,8 @@ def run_reference(args, rank, world):
 def run_voce(args, rank, world, grp):
     from voce_gb300 import capi, synth  # noqa: F401
     lib = capi.load()
-    prec = capi.PREC_MIXED if args.precision == "mixed" else capi.PREC_FP64
+    args.precision = args.precision or "fp64"
+    prec = PREC[args.precision]()
     case = make_case()
     nv = case.mesh.nvox
     d = tempfile.mkdtemp(prefix="bench_")
@@ -356,7 +381,7 @@ def run_voce(args, rank, world, grp):
         "metric": "voxel_iterations_per_s", "value": value, "unit": "voxel-iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if prec == capi.PREC_FP64 else "f64+f32fft",
+        "vs_baseline": None, "dtype": DTYPE[args.precision],
         "data": "synthetic",
         "config": {"workload": "64^3 periodic Voronoi, 125 grains, Cu FCC (C11=168.4 GPa), "
                                "n=20, Voce hardening, tension z 1e-3/s, 2e-4 strain per "
@@ -387,10 +412,12 @@ def run_voce(args, rank, world, grp):
 
 def run_cfg3(args):
     """256^3 periodic Voronoi (4096 grains), plane-strain compression: the
-    same increments in FP64 and in the mixed form; the mixed form's error
-    against FP64 on the macro stress curve and on the fields."""
+    same increments in FP64 and in both mixed forms; each mixed form's error
+    against FP64 on the macro stress curve and on the fields.  `value` is the
+    form --precision names (default mixed_nr32)."""
     import numpy as np
     from voce_gb300 import capi, synth
+    chosen = args.precision or "mixed_nr32"
     t0 = time.perf_counter()
     case = synth.config3(n_steps=250)
     t_mesh = time.perf_counter() - t0
@@ -402,8 +429,9 @@ def run_cfg3(args):
     slip = capi.read_slip(os.path.join(d, "mat.sx"))
     nv = case.mesh.nvox
     out = {}
-    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
-        r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase, prec)
+    for name in ("fp64", "mixed", "mixed_nr32"):
+        r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase,
+                            PREC[name]())
         r.run(args.warmup)
         ms, its = 0.0, 0
         for k in range(args.steps):
@@ -414,26 +442,36 @@ def run_cfg3(args):
         out[name] = {"value": nv * its / (ms * 1e-3), "ms": ms, "iters": its,
                      "incs": incs, "sig": r.field("sig_voigt"), "edot": r.field("edot_voigt")}
         r.close()
-    a, b = out["mixed"], out["fp64"]
+
     def rel(x, y):
-        x = np.asarray(x, float); y = np.asarray(y, float)
+        x = np.asarray(x, float)
+        y = np.asarray(y, float)
         return float(np.abs(x - y).max() / np.abs(y).max())
-    macro = max(rel(x["sig_avg"], y["sig_avg"]) for x, y in zip(a["incs"], b["incs"]))
+
+    b = out["fp64"]
+    forms = {"fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"]}}
+    for name in ("mixed", "mixed_nr32"):
+        a = out[name]
+        forms[name] = {
+            "value": a["value"], "ms_per_step": a["ms"] / args.steps, "iters": a["iters"],
+            "over_fp64": a["value"] / b["value"], "arithmetic": FORM_DOC[name],
+            "error_vs_fp64": {
+                "macro_stress_max_rel": max(rel(x["sig_avg"], y["sig_avg"])
+                                            for x, y in zip(a["incs"], b["incs"])),
+                "sigma_field_max_rel": rel(a["sig"], b["sig"]),
+                "edot_field_max_rel": rel(a["edot"], b["edot"]),
+                "green_iterations_vs_fp64": [a["iters"], b["iters"]]}}
+    a = out[chosen]
     res = {
         "metric": "voxel_iterations_per_s", "value": a["value"], "unit": "voxel-iter/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": a["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32fft", "data": "synthetic",
+        "vs_baseline": None, "dtype": DTYPE[chosen], "data": "synthetic",
         "config": {"workload": "256^3 periodic Voronoi, 4096 grains, Cu FCC, plane-strain "
                                "compression Lzz=-1e-3/s Lxx=+1e-3/s, 2e-4 per increment "
-                               "(config 3), mixed precision", "voxels": nv,
-                   "mesh_generation_s": t_mesh},
-        "fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"]},
-        "mixed_over_fp64": a["value"] / b["value"],
-        "mixed_error_vs_fp64": {"macro_stress_max_rel": macro,
-                                "sigma_field_max_rel": rel(a["sig"], b["sig"]),
-                                "edot_field_max_rel": rel(a["edot"], b["edot"]),
-                                "iterations_mixed_vs_fp64": [a["iters"], b["iters"]]},
+                               "(config 3), %s form" % chosen, "voxels": nv,
+                   "mesh_generation_s": t_mesh, "l2": "flushed before every step"},
+        "forms": forms,
     }
     print(json.dumps(res), flush=True)
 
@@ -473,11 +511,15 @@ def _plain_class_throughput(cases_by_edge, d):
 
 def run_cfg4(args):
     """Batched form: RVEs with edges drawn from {16,32,48,64}, grains
-    log-uniform 8-512, random traceless loads, 2.5e-4 per increment, FP32
-    FFT + FP64 flow rule, advanced in one batch (one launch per phase per
-    tick, tick loop as a CUDA graph).  Bounded sample: `--ticks` ticks."""
+    log-uniform 8-512, random traceless loads, 2.5e-4 per increment, advanced
+    in one batch (one launch per phase per tick, the tick loop a CUDA graph),
+    in both mixed forms; `value` is the form --precision names (default
+    mixed_nr32).  Bounded sample: `--ticks` ticks of every RVE.  Accuracy: one
+    RVE of each edge run through a whole increment in a batch of each form,
+    against the FP64 form alone."""
     import numpy as np
     from voce_gb300 import capi, synth
+    chosen = args.precision or "mixed_nr32"
     rng = np.random.Generator(np.random.PCG64(4))
     d = tempfile.mkdtemp(prefix="cfg4_")
     t0 = time.perf_counter()
@@ -490,71 +532,87 @@ def run_cfg4(args):
         cases.append(synth.Case("b%d" % i, mesh, synth.CU_LIKE, load, 0.25, 40))
     t_gen = time.perf_counter() - t0
     nv_tot = sum(c.mesh.nvox for c in cases)
-    t0 = time.perf_counter()
-    rves = []
-    for i, c in enumerate(cases):
-        nl, sx = _rve_inputs(c, d, str(i))
-        rves.append(capi.Rve.create(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase,
-                                    capi.PREC_MIXED))
-    t_setup = time.perf_counter() - t0
-    b = capi.Batch(capi.PREC_MIXED)
-    for r in rves:
-        b.add(r, 40)
-    b.run(max_ticks=3)                            # warm-up (graph build)
-    chunk = 20
-    done = 0
-    t0 = time.perf_counter()
-    while done < args.ticks:
-        left = b.run(max_ticks=min(chunk, args.ticks - done))
-        done += min(chunk, args.ticks - done)
-    t_run = time.perf_counter() - t0
-    value = nv_tot * args.ticks / t_run           # every RVE is active every tick (checked)
-    assert left == len(rves), left
-    # per-phase breakdown: a few more ticks driven from the host with every
-    # launch timed (after the timed region)
-    prof_ticks = 5
-    b.set_profiling(True)
-    b.reset_kernel_times()
-    b.run(max_ticks=prof_ticks)
-    kt = b.kernel_times()
-    b.set_profiling(False)
-    kernel_ms = {k: ms / prof_ticks for k, (ms, n) in kt.items() if n}
-    # accuracy: first increment of a few RVEs against the plain FP64 path alone
-    errs = []
-    for i in range(min(8, len(rves))):
-        if rves[i].increments_done < 1:
-            continue
-        c = cases[i]
-        nl, sx = _rve_inputs(c, d, "ref%d" % i)
-        with capi.Rve.create(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase) as rr:
-            rr.run(1)
-            a = np.array(rves[i].increment(0)["sig_avg"])
-            bb = np.array(rr.increment(0)["sig_avg"])
-            errs.append(float(np.abs(a - bb).max() / np.abs(bb).max()))
-    b.close()
-    for r in rves:
-        r.close()
-    by_edge = {}
-    for c in cases:
-        by_edge.setdefault(c.mesh.dims[0], c)
+    inputs = [_rve_inputs(c, d, str(i)) for i, c in enumerate(cases)]
+
+    def create(c, inp, prec):
+        return capi.Rve.create(inp[0], inp[1], c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, prec)
+
+    forms = {}
+    kernel_ms = {}
+    for name in (chosen, _other_mixed(chosen)):
+        prec = PREC[name]()
+        t0 = time.perf_counter()
+        rves = [create(c, inp, prec) for c, inp in zip(cases, inputs)]
+        t_setup = time.perf_counter() - t0
+        b = capi.Batch(prec)
+        for r in rves:
+            b.add(r, 40)
+        b.run(max_ticks=3)                            # warm-up (graph build)
+        chunk, done = 20, 0
+        t0 = time.perf_counter()
+        while done < args.ticks:
+            left = b.run(max_ticks=min(chunk, args.ticks - done))
+            done += min(chunk, args.ticks - done)
+        t_run = time.perf_counter() - t0
+        assert left == len(rves), left                # every RVE is active every tick
+        forms[name] = {"value": nv_tot * args.ticks / t_run, "ms_per_tick": 1e3 * t_run / args.ticks,
+                       "setup_s": t_setup, "arithmetic": FORM_DOC[name]}
+        if name == chosen:
+            # per-phase breakdown: more ticks driven from the host with every
+            # launch timed (after the timed region)
+            prof_ticks = 5
+            b.set_profiling(True)
+            b.reset_kernel_times()
+            b.run(max_ticks=prof_ticks)
+            kernel_ms = {k: ms / prof_ticks for k, (ms, n) in b.kernel_times().items() if n}
+            b.set_profiling(False)
+        b.close()
+        for r in rves:
+            r.close()
+    # accuracy: one RVE per edge, a whole first increment, batch vs FP64 alone
+    sample = {}
+    for c, inp in zip(cases, inputs):
+        sample.setdefault(c.mesh.dims[0], (c, inp))
+    for name in forms:
+        errs = {}
+        prec = PREC[name]()
+        rves = [create(c, inp, prec) for c, inp in sample.values()]
+        with capi.Batch(prec) as b:
+            for r in rves:
+                b.add(r, 1)
+            while b.run(max_ticks=200):
+                pass
+        for (edge, (c, inp)), r in zip(sample.items(), rves):
+            with create(c, inp, capi.PREC_FP64) as rr:
+                rr.run(1)
+                x = np.array(r.increment(0)["sig_avg"])
+                y = np.array(rr.increment(0)["sig_avg"])
+                errs[str(edge)] = float(np.abs(x - y).max() / np.abs(y).max())
+            r.close()
+        forms[name]["first_increment_macro_stress_err_vs_fp64"] = errs
+    by_edge = {e: c for e, (c, _) in sample.items()}
     thr = _plain_class_throughput(by_edge, d)
     t_plain = sum(c.mesh.nvox / thr[c.mesh.dims[0]] for c in cases)   # per iteration of all RVEs
     plain = nv_tot / t_plain
+    for f in forms.values():
+        f["batched_over_plain"] = f["value"] / plain
+    a = forms[chosen]
     res = {
-        "metric": "voxel_iterations_per_s", "value": value, "unit": "voxel-iter/s", "n_gpus": 1,
-        "steps": args.ticks, "warmup": 3, "ms_per_step": 1e3 * t_run / args.ticks,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32fft",
+        "metric": "voxel_iterations_per_s", "value": a["value"], "unit": "voxel-iter/s", "n_gpus": 1,
+        "steps": args.ticks, "warmup": 3, "ms_per_step": a["ms_per_tick"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[chosen],
         "data": "synthetic",
         "config": {"workload": "batched: %d RVEs, edges U{16,32,48,64}, grains log-U[8,512], "
                                "random traceless loads 1e-3/s, 2.5e-4 per increment (config 4), "
-                               "mixed precision, one batch tick per step" % len(cases),
-                   "voxels": nv_tot, "mesh_generation_s": t_gen, "setup_s": t_setup},
+                               "%s form, one batch tick per step" % (len(cases), chosen),
+                   "voxels": nv_tot, "mesh_generation_s": t_gen,
+                   "l2": "inputs larger than L2 (%.1f GB of RVE state)" % (
+                       sum(capi.footprint(c.mesh.dims, PREC[chosen]()) for c in cases) / 1e9)},
         "plain_fp64_one_at_a_time": {"value": plain, "per_edge": thr},
-        "batched_over_plain": value / plain,
+        "batched_over_plain": a["batched_over_plain"],
+        "forms": forms,
         "kernel_ms_per_tick": kernel_ms,
-        "kernel_timing": "CUDA events around every launch of %d host-driven ticks after the "
-                         "timed ones" % prof_ticks,
-        "first_increment_macro_err_vs_plain_fp64": errs,
+        "kernel_timing": "CUDA events around every launch of 5 host-driven ticks after the timed ones",
     }
     print(json.dumps(res), flush=True)
 
@@ -562,7 +620,7 @@ def run_cfg4(args):
 def run_cfg5(args):
     """Serving form: Poisson arrivals of RVE solve requests (edges
     U{16,32,64,128}, grains log-U[8,2048], random traceless loads), served
-    with continuous batching (mixed precision), against a plain-FP64 server
+    with continuous batching in both mixed forms, against a plain-FP64 server
     that solves one request at a time, on the same arrival trace."""
     import numpy as np
     from voce_gb300 import capi, synth
@@ -624,25 +682,32 @@ def run_cfg5(args):
                 vi += info.voxel_iterations
         return lat, vi, span
 
+    chosen = args.precision or "mixed_nr32"
     out = {}
-    for name, prec, single in (("served_mixed", capi.PREC_MIXED, False),
+    for name, prec, single in (("served_" + chosen, PREC[chosen](), False),
+                               ("served_" + _other_mixed(chosen), PREC[_other_mixed(chosen)](), False),
                                ("plain_fp64_one_at_a_time", capi.PREC_FP64, True)):
         lat, vi, span = serve(prec, single)
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "throughput": vi / span, "makespan_s": span, "voxel_iterations": vi}
-    a, b = out["served_mixed"], out["plain_fp64_one_at_a_time"]
+    b = out["plain_fp64_one_at_a_time"]
+    for name, a in out.items():
+        if name != "plain_fp64_one_at_a_time":
+            a.update(throughput_ratio=a["throughput"] / b["throughput"],
+                     p50_ratio=b["p50_s"] / a["p50_s"], p99_ratio=b["p99_s"] / a["p99_s"])
+    a = out["served_" + chosen]
     res = {
         "metric": "voxel_iterations_per_s", "value": a["throughput"], "unit": "voxel-iter/s",
         "n_gpus": 1, "steps": len(reqs), "warmup": 0, "ms_per_step": 1e3 * a["makespan_s"] / len(reqs),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32fft",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[chosen],
         "data": "synthetic",
         "config": {"workload": "serving: %d Poisson requests at %.2f req/s, edges U{16,32,64,128}, "
                                "grains log-U[8,2048], random traceless loads, increments "
                                "round(%.2f x U{10..80}) (config 5 sample), continuous batching, "
-                               "mixed precision" % (len(reqs), args.rate, args.inc_scale)},
-        "served": a, "plain_fp64_one_at_a_time": b,
-        "throughput_ratio": a["throughput"] / b["throughput"],
-        "p50_ratio": b["p50_s"] / a["p50_s"], "p99_ratio": b["p99_s"] / a["p99_s"],
+                               "%s form" % (len(reqs), args.rate, args.inc_scale, chosen)},
+        "served": out,
+        "throughput_ratio": a["throughput_ratio"], "p50_ratio": a["p50_ratio"],
+        "p99_ratio": a["p99_ratio"],
     }
     print(json.dumps(res), flush=True)
 

@@ -53,7 +53,17 @@ enum {
     VOCE_ERR_STATE = 9        /* call out of order */
 };
 
-enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1 };
+/* Precision forms.
+ *   VOCE_PREC_FP64        the reference's arithmetic: FP64 throughout.
+ *   VOCE_PREC_MIXED       spectrum and Green-operator convolution in FP32; the
+ *                         Newton-Raphson (the FP64 form's own code), the Voce
+ *                         hardening, the averages and the error norms in FP64.
+ *   VOCE_PREC_MIXED_NR32  as VOCE_PREC_MIXED, and the Newton iterations in
+ *                         FP32 ended by an acceptance step on the FP64
+ *                         residual (relative update below 1e-5), FP32-only
+ *                         while the Green error is above 1e-3; per-voxel error
+ *                         norms in FP32 (their sums in FP64). */
+enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1, VOCE_PREC_MIXED_NR32 = 2 };
 
 /* Every variable the reference's namelist reader knows (io.c:25-52), with
  * the reference's names, types and lengths. */

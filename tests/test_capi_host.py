@@ -86,7 +86,8 @@ def test_footprint_scales_with_grid(voce_lib):
     assert 7.9 < b / a < 8.1
     nv = 64 ** 3
     nspec = 33 * 64 * 64
-    # the mixed form keeps float copies of the Schmid vectors, 1/crss and S_g + S0 (+420 B/voxel)
-    # and holds the 9 spectra in complex<float> (8 B instead of 16)
-    assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a + 420 * nv - 9 * 8 * nspec
+    # the mixed forms hold the spectrum in FP32; the single-precision Newton
+    # form also keeps float copies of the Schmid vectors, 1/crss and S_g + S0
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 420 * nv - 9 * 8 * nspec
     assert capi.footprint((256, 256, 256)) < 40e9

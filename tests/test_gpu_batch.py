@@ -42,7 +42,7 @@ def _same(a, b):
         assert np.array_equal(u, v)
 
 
-@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32])
 def test_alone_equals_in_batch(prec, voce_lib):
     cases = _cases()
     alone = []
@@ -94,8 +94,8 @@ def test_profiled_ticks_equal_graph_ticks(voce_lib):
     cases = _cases()[:4]
     snaps = []
     for prof in (False, True):
-        rves = [_make(c, capi.PREC_MIXED) for c, _ in cases]
-        with capi.Batch(capi.PREC_MIXED) as b:
+        rves = [_make(c, capi.PREC_MIXED_NR32) for c, _ in cases]
+        with capi.Batch(capi.PREC_MIXED_NR32) as b:
             for r, (c, n) in zip(rves, cases):
                 b.add(r, n)
             if prof:

@@ -1,7 +1,8 @@
-"""The mixed-precision form (VOCE_PREC_MIXED: single-precision spectrum,
-Green operator and Newton iterations, double-precision residual acceptance,
-hardening, norms and averages) against the reference's own macro curve and
-fields (golden fixtures) and against the FP64 form on the GPU.
+"""The mixed-precision forms against the reference's own macro curve and
+fields (golden fixtures) and against the FP64 form on the GPU:
+VOCE_PREC_MIXED (FP32 spectrum and Green operator, FP64 Newton, hardening,
+norms and averages) and VOCE_PREC_MIXED_NR32 (the same with FP32 Newton
+iterations ended by an FP64-residual acceptance step).
 
 Bounds: the macro stress / strain / strain-rate averages of every increment
 within 1e-4 relative (the bound the mixed form is held to); per-voxel stress
@@ -28,8 +29,12 @@ def _write(case):
     return case.write(tempfile.mkdtemp(prefix="mixed_"))
 
 
+FORMS = [capi.PREC_MIXED, capi.PREC_MIXED_NR32]
+
+
+@pytest.mark.parametrize("prec", FORMS)
 @pytest.mark.parametrize("name", CASES)
-def test_mixed_matches_reference_macro_curve(name, voce_lib):
+def test_mixed_matches_reference_macro_curve(name, prec, voce_lib):
     if not gio.available(name):
         pytest.skip("fixture not generated")
     make, n, _ = make_golden.CASES[name]
@@ -38,7 +43,7 @@ def test_mixed_matches_reference_macro_curve(name, voce_lib):
     assert case.mesh.digest() == str(fx["digest"])
     seg = gio.segment(fx, case.update_flag)
     nv = case.mesh.nvox
-    with capi.Rve.from_files(_write(case), capi.PREC_MIXED) as r:
+    with capi.Rve.from_files(_write(case), prec) as r:
         r.run(n)
         worst = 0.0
         for k in range(n):
@@ -58,19 +63,20 @@ def test_mixed_matches_reference_macro_curve(name, voce_lib):
         sig, edot = sig[idx], edot[idx]
     assert gio.rel(sig, fx["sig"]) < FIELD_TOL
     assert gio.rel(edot, fx["edot"]) < FIELD_TOL
-    print(name, "worst macro rel", worst)
+    print(name, prec, "worst macro rel", worst)
 
 
-def test_mixed_vs_fp64_random_load(voce_lib):
+@pytest.mark.parametrize("prec", FORMS)
+def test_mixed_vs_fp64_random_load(prec, voce_lib):
     rng = np.random.Generator(np.random.PCG64(77))
     case = synth.small_case(24, 30, 77, n_steps=3, load=synth.random_traceless_load(rng))
     out = {}
-    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
-        with capi.Rve.from_files(_write(case), prec) as r:
+    for p in (capi.PREC_FP64, prec):
+        with capi.Rve.from_files(_write(case), p) as r:
             r.run(3)
-            out[prec] = ([r.increment(k) for k in range(3)], r.field("sig_voigt"),
+            out[p] = ([r.increment(k) for k in range(3)], r.field("sig_voigt"),
                          r.field("edot_voigt"), r.field("crss"))
-    (i64, s64, e64, c64), (i32, s32, e32, c32) = out[capi.PREC_FP64], out[capi.PREC_MIXED]
+    (i64, s64, e64, c64), (i32, s32, e32, c32) = out[capi.PREC_FP64], out[prec]
     for a, b in zip(i32, i64):
         assert gio.rel(np.array(a["sig_avg"]), np.array(b["sig_avg"])) < MACRO_TOL
         assert abs(a["iters"] - b["iters"]) <= max(2, 0.1 * b["iters"])

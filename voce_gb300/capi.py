@@ -21,7 +21,7 @@ VOCE_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
           5: "ERR_SINGULAR", 6: "ERR_UNSUPPORTED", 7: "ERR_NOMEM", 8: "ERR_CUDA",
           9: "ERR_STATE"}
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_NR32 = 0, 1, 2
 NOALLOC_MAX_DOUBLES = 4194304   # VOCE_NOALLOC_MAX_DOUBLES
 # .iout dump kinds (include/voce_io.h)
 IOUT = {"eps": 0, "sig": 1, "els": 2, "edot": 3, "slip": 4, "taux": 5, "crss": 6, "tex": 7,

@@ -412,11 +412,11 @@ long long voce_rve_footprint(const int dims[3], int precision)
 {
     const long long nv = (long long)dims[0] * dims[1] * dims[2];
     const long long nspec = (long long)(dims[2] / 2 + 1) * dims[0] * dims[1];
-    const long long cplx = precision == VOCE_PREC_MIXED ? 8 : 16;
+    const long long cplx = precision == VOCE_PREC_FP64 ? 16 : 8;
     // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
-    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED ? 420 : 0)) + nspec * 9 * cplx;
+    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 420 : 0)) + nspec * 9 * cplx;
 }
 
 // ---------------------------------------------------------------------------
@@ -457,14 +457,19 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
             return fail(VOCE_ERR_PARSE, "phase id %d at voxel %lld", mesh->phase[v], v);
 
     voce_rve *r = new voce_rve();
-    r->precision = precision == VOCE_PREC_MIXED ? 1 : 0;
+    if (precision != VOCE_PREC_FP64 && precision != VOCE_PREC_MIXED && precision != VOCE_PREC_MIXED_NR32) {
+        delete r;
+        return fail(VOCE_ERR_ARG, "unknown precision %d", precision);
+    }
+    r->precision = precision;
     RveDesc &d = r->d;
     SetupConst &sc = r->sc;
     d.nx = nx; d.ny = ny; d.nz = nz; d.nzh = nz / 2 + 1;
     d.nv = nv;
     d.nspec = (long long)d.nzh * nx * ny;
     d.plx = plx; d.ply = ply; d.plz = plz;
-    d.mixed = r->precision;
+    d.mixed = r->precision != VOCE_PREC_FP64;
+    d.nr32 = r->precision == VOCE_PREC_MIXED_NR32;
     for (int p = 0; p < 2; ++p) d.solid[p + 1] = (p < nl->N_phases && !nl->Type_phases[p]) ? 1 : 0;
     d.nsys = sx.nsys;
     d.update_flag = nl->Update_Flag;
@@ -576,7 +581,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     // and precision.
     const long long sm_count = 152;
     long long nb = (nv + 127) / 128;
-    const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(r->precision != 0));
+    const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(d.nr32 != 0));
     r->npart = (int)(nb < cap ? nb : cap);
     d.npart = r->npart;
     int rc = VOCE_OK;
@@ -588,13 +593,13 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     d.sch32 = nullptr;
     d.itau32 = nullptr;
     d.sgp32 = nullptr;
-    if (r->precision) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
+    if (d.nr32) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
     AL(d.macro, 1);
     d.incr_cap = 32;   // increments per host read-back
     AL(d.itlog, (size_t)d.incr_cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
     AL(d.incr, d.incr_cap);
-    const size_t csz = r->precision ? sizeof(float2) : sizeof(double2);
+    const size_t csz = d.mixed ? sizeof(float2) : sizeof(double2);
     {
         char *p;
         AL(p, 6 * d.nspec * csz); d.spec = p;
@@ -644,7 +649,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     if (!lu_inv66(S066)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066"); }
     std::memcpy(d.S0, S066, sizeof(S066));
     for (int q = 0; q < 36; ++q) d.S0f[q] = (float)d.S0[q];
-    if (r->precision) CUDA_TRY(launch_fill_p32(d, r->stream));
+    if (d.nr32) CUDA_TRY(launch_fill_p32(d, r->stream));
     double C0t[81];
     c66_to_t4(&C066[0][0], C0t);
     c66_to_t4(&S066[0][0], d.S0t);
@@ -686,7 +691,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     m.Err_e = 2. * d.err_tol;
     m.Err_s = 2. * d.err_tol;
     CUDA_TRY(cudaMemcpyAsync(d.macro, &m, sizeof(m), cudaMemcpyHostToDevice, r->stream));
-    if (r->precision) r->tiles.choose<float>(d);
+    if (d.mixed) r->tiles.choose<float>(d);
     else r->tiles.choose<double>(d);
     d.zrows = r->tiles.zrows; d.yxt = r->tiles.yxt; d.xkc = r->tiles.xkc;
     d.xkc3 = r->tiles.xkc3; d.zirows = r->tiles.zirows; d.zirows3 = r->tiles.zirows3;
@@ -754,7 +759,8 @@ void collect_increment(voce_rve *r, const IncrDev &rec, const double *log_rows)
 }
 
 // Work lists and descriptor array of a set of RVEs (device memory).
-int make_plan(const std::vector<RveDesc> &descs, bool mixed, RveDesc *&d_descs, int2 *&d_maps, BatchPlan &p)
+int make_plan(const std::vector<RveDesc> &descs, int precision, RveDesc *&d_descs, int2 *&d_maps,
+              BatchPlan &p)
 {
     if (d_descs) cudaFree(d_descs);
     if (d_maps) cudaFree(d_maps);
@@ -763,7 +769,8 @@ int make_plan(const std::vector<RveDesc> &descs, bool mixed, RveDesc *&d_descs, 
     int *ticks = p.ticks, *maxt = p.max_ticks, *act = p.active_out;
     p = BatchPlan();
     p.ticks = ticks; p.max_ticks = maxt; p.active_out = act;
-    p.mixed = mixed;
+    p.mixed = precision != VOCE_PREC_FP64;
+    p.nr32 = precision == VOCE_PREC_MIXED_NR32;
     p.nrve = (int)descs.size();
     if (descs.empty()) return VOCE_OK;
     std::vector<std::vector<int2>> maps(BP_COUNT);
@@ -796,7 +803,7 @@ int ensure_self_plan(voce_rve *r)
 {
     if (!r->plan_dirty) return VOCE_OK;
     std::vector<RveDesc> one(1, r->d);
-    int rc = make_plan(one, r->precision != 0, r->plan_desc, r->plan_maps, r->plan);
+    int rc = make_plan(one, r->precision, r->plan_desc, r->plan_maps, r->plan);
     if (rc) return rc;
     r->plan_dirty = false;
     return VOCE_OK;
@@ -1266,14 +1273,15 @@ int build_batch(voce_batch *b)
     BatchPlan &p = b->plan;
     p = BatchPlan();
     p.nrve = n;
-    p.mixed = b->precision != 0;
+    p.mixed = b->precision != VOCE_PREC_FP64;
+    p.nr32 = b->precision == VOCE_PREC_MIXED_NR32;
     if (n == 0) { b->dirty = false; return VOCE_OK; }
     std::vector<RveDesc> descs(n);
     for (int i = 0; i < n; ++i) descs[i] = b->rves[i]->d;
     p.ticks = b->d_ctl;
     p.max_ticks = b->d_ctl + 1;
     p.active_out = b->d_ctl + 2;
-    int rc = make_plan(descs, b->precision != 0, b->d_descs, b->d_maps, p);
+    int rc = make_plan(descs, b->precision, b->d_descs, b->d_maps, p);
     if (rc) return rc;
     // graph: WHILE (any RVE active and ticks < max) { tick }
     cudaGraph_t g;
@@ -1305,7 +1313,11 @@ int voce_batch_create(int precision, voce_batch **out)
 {
     if (!out) return fail(VOCE_ERR_ARG, "null argument");
     voce_batch *b = new voce_batch();
-    b->precision = precision == VOCE_PREC_MIXED ? 1 : 0;
+    if (precision != VOCE_PREC_FP64 && precision != VOCE_PREC_MIXED && precision != VOCE_PREC_MIXED_NR32) {
+        delete b;
+        return fail(VOCE_ERR_ARG, "unknown precision %d", precision);
+    }
+    b->precision = precision;
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ctl, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_ctl, 4 * sizeof(int));

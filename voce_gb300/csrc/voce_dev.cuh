@@ -79,6 +79,7 @@ struct RveDesc {
     int nsys, ipow_n;    // ipow_n >= 0: n integral, |r|^(n-1) by multiplication
     int update_flag, hard_flag, creep, iter_max;
     int mixed;           // spectrum precision: 0 double, 1 float
+    int nr32;            // Newton iterations in float with an FP64 acceptance step
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
     float gam0f[VOCE_NS], nrsf[VOCE_NS];   // float copies for the mixed Newton

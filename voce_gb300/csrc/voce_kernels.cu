@@ -471,7 +471,8 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
 // solved in the equivalent symmetric form
 //   (S0 + S_g + dt dEdot) dsig = S0 R
 // where R is the reference's residual (evolution.c:78-83) and S0 = C0^-1.
-// MIXED_NR: see mixed_newton below.
+// NR32 (the VOCE_PREC_MIXED_NR32 form): see mixed_newton below; otherwise
+// the FP64 Newton of the reference, for the FP64 and VOCE_PREC_MIXED forms.
 // ---------------------------------------------------------------------------
 
 // P = S_g + S0 (packed upper triangle) of voxel v
@@ -502,10 +503,11 @@ __device__ __forceinline__ void reload_P(const RveDesc &d, long long v, double (
         for (int j = i; j < 6; ++j) P[sym6(i, j)] += d.S0[i * 6 + j];
 }
 
-// Newton steps on the FP64 residual with an FP32 Jacobian and solve (an
-// inexact Newton step converging to the same FP64 fixed point); the loop of
-// the FP64 form with the stop test of evolution.c:112.
-template <bool MIXED_NR>
+// Newton steps on the FP64 residual with the stop test of evolution.c:112.
+// NR32 (fallback of the single-precision form only): the Jacobian and its
+// solve in FP32, an inexact Newton step converging to the same FP64 fixed
+// point; otherwise all FP64.
+template <bool NR32>
 __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const double (&P)[21],
                                            const double (&cc)[6], double thr, double (&sig)[6],
                                            double (&sp)[6], double (&Rl)[6], int &it)
@@ -518,7 +520,7 @@ __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const
 #pragma unroll
         for (int c = 0; c < 6; ++c) sp[c] = sig[c];
         double R[6];
-        if (MIXED_NR) {
+        if (NR32) {
             float D[15];
             flow_rule<true, false, float>(d, v, sig, ed, D, nullptr, nullptr);
             float M[6][6], x[6];
@@ -714,7 +716,7 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
     }
 }
 
-template <bool MIXED_NR>
+template <bool NR32>
 __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 {
     // per-thread sums in shared memory (one slot per thread, the same
@@ -723,7 +725,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     __shared__ double s_acc[VOCE_NPART][128];
     const int tid = threadIdx.x;
     bool polish = true;
-    if (MIXED_NR) {
+    if (NR32) {
         const MacroDev *m = d.macro;
         polish = !m->first_iter && fmax(fabs(m->Err_e), fabs(m->Err_s)) <= VOCE_POLISH_ERR;
     }
@@ -764,7 +766,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 #pragma unroll
         for (int c = 0; c < 6; ++c) { sig[c] = lam[c]; sp[c] = lam[c]; Rl[c] = 0.0; }
         int it = 0;
-        if (MIXED_NR) {
+        if (NR32) {
             mixed_newton(d, v, lam, cc, sn2, polish, sig, sp, Rl, it);
         } else {
             double P[21];
@@ -773,7 +775,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             newton_fp64<false>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
         }
         double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
-        if (MIXED_NR) {
+        if (NR32) {
             // error norms in single precision: they only steer the Green
             // iteration's stop test at 1e-5
             float ds[6], dp[6], cs = 0.0f, ce = 0.0f;
@@ -873,7 +875,7 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
     // the mixed form's Newton ran in single precision alone this iteration
     // (the predicate nr_unit used): it may not end the increment
     const bool fp32_only =
-        d.mixed && (m->first_iter || fmax(fabs(m->Err_e), fabs(m->Err_s)) > VOCE_POLISH_ERR);
+        d.nr32 && (m->first_iter || fmax(fabs(m->Err_e), fabs(m->Err_s)) > VOCE_POLISH_ERR);
     double Err_e = tot[1] * d.wgt, Err_s = tot[0] * d.wgt;
     double s9[9], s19[9];
     sym9_from_b(tot + 2, s9);
@@ -1394,21 +1396,21 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
     }
 }
 
-// resident blocks of 128 threads per SM the mixed Newton kernel is compiled
-// for (register budget 65536 / (128 x blocks))
+// resident blocks of 128 threads per SM the single-precision Newton kernel
+// (kb_nr<true>) is compiled for (register budget 65536 / (128 x blocks))
 #ifndef VOCE_NR_MIXED_BLOCKS
 #define VOCE_NR_MIXED_BLOCKS 3
 #endif
 
-template <bool MIXED_NR>
-__global__ void __launch_bounds__(128, MIXED_NR ? VOCE_NR_MIXED_BLOCKS : 1)
+template <bool NR32>
+__global__ void __launch_bounds__(128, NR32 ? VOCE_NR_MIXED_BLOCKS : 1)
 kb_nr(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
         if (!unit_on(d, MASK_ACTIVE)) continue;
-        nr_unit<MIXED_NR>(d, e.y, d.npart);
+        nr_unit<NR32>(d, e.y, d.npart);
     }
 }
 
@@ -1553,15 +1555,15 @@ cudaError_t set_batch_smem(const BatchPlan &bp)
 
 // Newton-kernel blocks resident per GPU (SMs x blocks per SM): the grid cap
 // of kb_nr and the most units an RVE is split into for it
-int nr_resident_blocks(bool mixed)
+int nr_resident_blocks(bool nr32)
 {
     static int cached[2] = {0, 0};
-    int &c = cached[mixed ? 1 : 0];
+    int &c = cached[nr32 ? 1 : 0];
     if (!c) {
         int dev = 0, sms = 152, per = 2;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, 128, 0);
+        if (nr32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, 128, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, 128, 0);
         c = sms * (per > 0 ? per : 1);
     }
@@ -1604,7 +1606,7 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
     pf.end(K_FFT_Z_INV, s);
     pf.begin(K_NR, s);
-    if (bp.mixed)
+    if (bp.nr32)
         kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), 128, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else

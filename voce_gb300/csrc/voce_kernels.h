@@ -62,7 +62,8 @@ struct BatchPlan {
     int total[BP_COUNT] = {};
     size_t smem[BP_COUNT] = {};       // dynamic shared memory of the FFT phases
     int *ticks = nullptr, *max_ticks = nullptr, *active_out = nullptr;
-    bool mixed = false;
+    bool mixed = false;   // float spectrum
+    bool nr32 = false;    // float Newton iterations (kb_nr<true>)
 };
 // units of one RVE in each phase
 void batch_units(const RveDesc &d, int units[BP_COUNT]);
@@ -84,7 +85,7 @@ cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
 // the mixed form's float (S_g + S0), once S0 is set in d
 cudaError_t launch_fill_p32(const RveDesc &d, cudaStream_t s);
 // kb_nr blocks resident on the current GPU (SMs x blocks per SM)
-int nr_resident_blocks(bool mixed);
+int nr_resident_blocks(bool nr32);
 double measure_fp64_tflops();
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s);
