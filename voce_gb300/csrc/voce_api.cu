@@ -467,6 +467,11 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     d.nx = nx; d.ny = ny; d.nz = nz; d.nzh = nz / 2 + 1;
     d.nv = nv;
     d.nspec = (long long)d.nzh * nx * ny;
+    const int dims3[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+        d.inv_n[a] = 1.0 / dims3[a];
+        d.inv_nf[a] = (float)(1.0 / dims3[a]);
+    }
     d.plx = plx; d.ply = ply; d.plz = plz;
     d.mixed = r->precision != VOCE_PREC_FP64;
     d.nr32 = r->precision == VOCE_PREC_MIXED_NR32;
@@ -662,6 +667,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
                 double v = C0t[((i * 3 + j) * 3 + k) * 3 + l];
                 if (j != l) v += C0t[((i * 3 + l) * 3 + k) * 3 + j];
                 d.Kq[a * 6 + m] = v;
+                d.Kqf[a * 6 + m] = (float)v;
             }
     }
     // macro state (InitFields init.c:494-499, 536; Evolution locals)

@@ -91,6 +91,9 @@ struct RveDesc {
     float S0f[36];       // float copy (mixed-precision error norms)
     double S0t[81];      // S0 as 3x3x3x3 (get_smacro's dDisGradAvg)
     double Kq[36];       // acoustic tensor coefficients: K6 = Kq * nn6
+    float Kqf[36];       // float copy (Green operator of the mixed forms)
+    double inv_n[3];     // 1.0/nx, 1.0/ny, 1.0/nz
+    float inv_nf[3];
     double Udot[9], Scauchy[9];
     double u6[6];        // B-basis sym(Udot)
     double ua[3];        // antisym(Udot): A12, A02, A01
@@ -392,47 +395,74 @@ __device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)
 // the reference maps index N/2 to -pi for both k and -k (init.c:661-666);
 // there both operators are applied and averaged.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double kfreq(int i, int n)
+// Frequency of index i on an axis of n points (init.c:655-666): the
+// reference's i/n - round(i/n), scaled by its 2 pi; inv_n = 1.0/n exactly as
+// the host computes it.
+__device__ __forceinline__ double kfreq(int i, double inv_n)
 {
-    double t = (double)i * (double)(1.0 / n);
+    double t = (double)i * inv_n;
     t -= round(t);
     return t * VOCE_TWO_PI_REF;
 }
 
-__device__ __forceinline__ void unit_freq(int ix, int iy, int iz, int nx, int ny, int nz, double *n)
+// The same in single precision, with the rounding done on the integer index
+// (i in [0, n): i - n when 2i >= n, which is where round(i/n) is 1).
+__device__ __forceinline__ float kfreqf(int i, int n, float inv_n)
 {
-    double g0 = kfreq(ix, nx), g1 = kfreq(iy, ny), g2 = kfreq(iz, nz);
-    double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
-    double s = 1.0 / gn;
+    const int ii = (2 * i >= n) ? i - n : i;
+    return ((float)ii * inv_n) * (float)VOCE_TWO_PI_REF;
+}
+
+// Unit frequency vector n = g/|g| (g != 0)
+__device__ __forceinline__ void unit_freq(const RveDesc &d, int ix, int iy, int iz, double *n)
+{
+    const double g0 = kfreq(ix, d.inv_n[0]), g1 = kfreq(iy, d.inv_n[1]), g2 = kfreq(iz, d.inv_n[2]);
+    const double s = rsqrt(g0 * g0 + g1 * g1 + g2 * g2);
     n[0] = g0 * s; n[1] = g1 * s; n[2] = g2 * s;
 }
 
-template <typename R>
-__device__ __forceinline__ void green_rank1(const double *Kq, const double *nd,
+__device__ __forceinline__ void unit_freq(const RveDesc &d, int ix, int iy, int iz, float *n)
+{
+    const float g0 = kfreqf(ix, d.nx, d.inv_nf[0]), g1 = kfreqf(iy, d.ny, d.inv_nf[1]);
+    const float g2 = kfreqf(iz, d.nz, d.inv_nf[2]);
+    const float s = rsqrtf(g0 * g0 + g1 * g1 + g2 * g2);
+    n[0] = g0 * s; n[1] = g1 * s; n[2] = g2 * s;
+}
+
+// Arithmetic type of the Green operator: double in the FP64 form, float with
+// the single-precision spectrum (the mixed forms).
+template <typename R> struct GreenT { typedef double T; };
+template <> struct GreenT<float> { typedef float T; };
+
+__device__ __forceinline__ double green_rcp(double x) { return rcp_nr(x); }
+__device__ __forceinline__ float green_rcp(float x) { return __frcp_rn(x); }
+
+template <typename R, typename G>
+__device__ __forceinline__ void green_rank1(const G *Kq, const G *nd,
                                             const R (&sr)[6], const R (&si)[6],
                                             R (&ur)[6], R (&ui)[6], R (&ar)[3], R (&ai)[3],
                                             R wgt)
 {
     // acoustic tensor K_ik = C0_ijkl n_j n_l (6 sym comps) = Kq * nn
-    double nn[6] = {nd[0] * nd[0], nd[1] * nd[1], nd[2] * nd[2],
-                    nd[1] * nd[2], nd[0] * nd[2], nd[0] * nd[1]};
-    double K[6];
+    G nn[6] = {nd[0] * nd[0], nd[1] * nd[1], nd[2] * nd[2],
+               nd[1] * nd[2], nd[0] * nd[2], nd[0] * nd[1]};
+    G K[6];
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
-        double s = 0.0;
+        G s = G(0);
 #pragma unroll
         for (int m = 0; m < 6; ++m) s = fma(Kq[a * 6 + m], nn[m], s);
         K[a] = s;
     }
     // omega = K^-1 by cofactors (M3Inverse, init.c:546-568); K symmetric
-    double c00 = K[1] * K[2] - K[3] * K[3];
-    double c01 = K[4] * K[3] - K[5] * K[2];
-    double c02 = K[5] * K[3] - K[4] * K[1];
-    double c11 = K[0] * K[2] - K[4] * K[4];
-    double c12 = K[4] * K[5] - K[0] * K[3];
-    double c22 = K[0] * K[1] - K[5] * K[5];
-    double det = K[0] * c00 + K[5] * c01 + K[4] * c02;
-    double id = 1.0 / det;
+    G c00 = K[1] * K[2] - K[3] * K[3];
+    G c01 = K[4] * K[3] - K[5] * K[2];
+    G c02 = K[5] * K[3] - K[4] * K[1];
+    G c11 = K[0] * K[2] - K[4] * K[4];
+    G c12 = K[4] * K[5] - K[0] * K[3];
+    G c22 = K[0] * K[1] - K[5] * K[5];
+    G det = K[0] * c00 + K[5] * c01 + K[4] * c02;
+    G id = green_rcp(det);
     R w00 = R(c00 * id), w01 = R(c01 * id), w02 = R(c02 * id);
     R w11 = R(c11 * id), w12 = R(c12 * id), w22 = R(c22 * id);
     R n0 = R(nd[0]), n1 = R(nd[1]), n2 = R(nd[2]);
@@ -457,6 +487,9 @@ __device__ __forceinline__ void green_rank1(const double *Kq, const double *nd,
     ar[2] += hh * (v0r * n1 - v1r * n0);   ai[2] += hh * (v0i * n1 - v1i * n0);
 }
 
+__device__ __forceinline__ const double *green_kq(const RveDesc &d, double *) { return d.Kq; }
+__device__ __forceinline__ const float *green_kq(const RveDesc &d, float *) { return d.Kqf; }
+
 // Apply the Green operator at frequency (ix,iy,iz).  In: B-basis stress
 // spectrum (br, bi).  Out: B-basis symmetric update in (br, bi) and the
 // antisymmetric update (ar, ai).
@@ -472,17 +505,19 @@ __device__ __forceinline__ void green_apply(const RveDesc &d, int ix, int iy, in
 #pragma unroll
     for (int a = 0; a < 3; ++a) { ar[a] = R(0); ai[a] = R(0); }
     if ((ix | iy | iz) != 0) {
-        double n[3];
-        unit_freq(ix, iy, iz, d.nx, d.ny, d.nz, n);
+        typedef typename GreenT<R>::T G;
+        const G *kq = green_kq(d, (G *)nullptr);
+        G n[3];
+        unit_freq(d, ix, iy, iz, n);
         bool nyq = ((d.nx % 2 == 0) && ix == d.nx / 2) || ((d.ny % 2 == 0) && iy == d.ny / 2) ||
                    ((d.nz % 2 == 0) && iz == d.nz / 2);
         if (!nyq) {
-            green_rank1<R>(d.Kq, n, sr, si, ur, ui, ar, ai, R(1));
+            green_rank1<R, G>(kq, n, sr, si, ur, ui, ar, ai, R(1));
         } else {
-            double n2[3];
-            unit_freq((d.nx - ix) % d.nx, (d.ny - iy) % d.ny, (d.nz - iz) % d.nz, d.nx, d.ny, d.nz, n2);
-            green_rank1<R>(d.Kq, n, sr, si, ur, ui, ar, ai, R(0.5));
-            green_rank1<R>(d.Kq, n2, sr, si, ur, ui, ar, ai, R(0.5));
+            G n2[3];
+            unit_freq(d, (d.nx - ix) % d.nx, (d.ny - iy) % d.ny, (d.nz - iz) % d.nz, n2);
+            green_rank1<R, G>(kq, n, sr, si, ur, ui, ar, ai, R(0.5));
+            green_rank1<R, G>(kq, n2, sr, si, ur, ui, ar, ai, R(0.5));
         }
     }
     t6_to_b<R>(ur, br);
