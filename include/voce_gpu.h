@@ -61,7 +61,7 @@ enum {
  *   VOCE_PREC_MIXED_NR32  as VOCE_PREC_MIXED, and the Newton iterations in
  *                         FP32 ended by an acceptance step on the FP64
  *                         residual (relative update below 1e-5), FP32-only
- *                         while the Green error is above 1e-3; per-voxel error
+ *                         while the Green error is above 1e-4; per-voxel error
  *                         norms in FP32 (their sums in FP64). */
 enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1, VOCE_PREC_MIXED_NR32 = 2 };
 

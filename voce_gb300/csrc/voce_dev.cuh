@@ -31,7 +31,7 @@
 // Mixed form: Green iterations whose predecessor's normalised error is above
 // this (and the first of every increment) run the Newton solve in single
 // precision only; the rest end it on the double-precision residual.
-#define VOCE_POLISH_ERR 1e-3
+#define VOCE_POLISH_ERR 1e-4
 
 // Lebensohn-Tome basis constants, the literal values of kinematics.c:333-335
 #define RSQ2 0.70710678118654744

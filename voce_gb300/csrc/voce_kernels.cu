@@ -620,7 +620,11 @@ __device__ __forceinline__ void edot_fp64(const RveDesc &d, long long v, const d
 // next update near 1e-9, under the 1e-7 test of the FP64 form, so the
 // accepted stress is taken as the converged point (zero residual, and the
 // point the strain rate is later evaluated at).  Anything else continues with
-// newton_fp64 from where it stands.
+// newton_fp64 from where it stands.  Without polish (Green iterations whose
+// predecessor's error is above VOCE_POLISH_ERR, and the first of an
+// increment) the single-precision Newton runs down to 1e-5 and its point is
+// taken as converged: its error, a few 1e-6 relative, is far below the
+// change such an iteration makes.
 __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, const double (&lam)[6],
                                              const double (&cc)[6], double sn2, bool polish,
                                              double (&sig)[6], double (&sp)[6], double (&Rl)[6],
