@@ -184,30 +184,33 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the Newton kernel from the committed ncu
-    summary (profiles/ncu_traffic.json), scaled to 64^3 by voxel count."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if not os.path.exists(p):
-        return None
-    d = json.load(open(p))
-    k = d.get("k_nr")
-    if not k:
-        return None
-    return float(k["dram_bytes_per_launch"]) * (64 ** 3) / float(k["voxels"])
+# From the ncu capture of kb_nr<0> (FP64 form) on this workload, summarised in
+# profiles/kb_nr_fp64_cfg2_64.md: DRAM bytes read + written by one launch over
+# 262144 voxels, and the FP64 flops (FMA = 2) per Newton iteration of a voxel
+# and per voxel per launch (instruction counts fitted against the Newton
+# iterations of each launch; the capture there checks the fit).
+KB_NR_FP64_DRAM_BYTES = 269.4e6
+KB_NR_FP64_VOXELS = 262144
+KB_NR_FP64_FLOPS_PER_NEWTON = 1127
+KB_NR_FP64_FLOPS_PER_VOXEL = 307
+
+
+# The same for kb_nr<1> (mixed_nr32 form, profiles/kb_nr_nr32_cfg2_64.md); the
+# mixed form runs the FP64 form's Newton kernel.
+KB_NR_NR32_DRAM_BYTES = 387.5e6
+
+
+def profiled_traffic(precision="fp64"):
+    """DRAM bytes of one Newton launch at 64^3, from the ncu capture of the
+    kernel the form runs."""
+    b = KB_NR_NR32_DRAM_BYTES if precision == "mixed_nr32" else KB_NR_FP64_DRAM_BYTES
+    return b * (64 ** 3) / KB_NR_FP64_VOXELS
 
 
 def fp64_flops_per_newton_iteration():
-    """FP64 flops (FMA = 2) that k_nr executes per Newton iteration of one
-    voxel and per voxel per launch, from the committed ncu instruction
-    counts (plain FP64 kernel)."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if not os.path.exists(p):
-        return None
-    k = json.load(open(p)).get("k_nr", {})
-    if "fp64_flops_per_newton_iteration" not in k:
-        return None
-    return k["fp64_flops_per_newton_iteration"], k.get("fp64_flops_per_voxel_launch", 0.0)
+    """FP64 flops (FMA = 2) that kb_nr<0> executes per Newton iteration of
+    one voxel and per voxel per launch (profiles/kb_nr_fp64_cfg2_64.md)."""
+    return KB_NR_FP64_FLOPS_PER_NEWTON, KB_NR_FP64_FLOPS_PER_VOXEL
 
 
 def cpu_sample(threads: int, iters: int):
@@ -391,11 +394,11 @@ def run_voce(args, rank, world, grp):
                    "green_iterations": iters, "l2": "flushed (512 MB write) before every step",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic(),
-                     "kernel": "k_nr", "peak_kind": peak_kind,
+                     "frac": achieved / peak, "traffic": profiled_traffic(args.precision),
+                     "kernel": "kb_nr", "peak_kind": peak_kind,
                      "algorithmic_bytes_per_voxel": NR_BYTES_PER_VOXEL,
                      "avg_launch_ms": nr_avg_s * 1e3},
-        "fp64_roof": {"bound": "fp64", "kernel": "k_nr", "achieved": fp64_ach,
+        "fp64_roof": {"bound": "fp64", "kernel": "kb_nr", "achieved": fp64_ach,
                       "peak": fp64_peak, "unit": "TFLOP/s",
                       "frac": (fp64_ach / fp64_peak) if fp64_ach else None,
                       "peak_kind": "measured by voce_measure_fp64_tflops in this run"},
