@@ -201,6 +201,21 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out);
 #define VOCE_NOALLOC_MAX_DOUBLES 4194304
 int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out);
 
+/* Snapshot / restore (no counterpart in the reference, which has no resume:
+ * its io.c dumps are write-only).  A snapshot holds everything an RVE
+ * carries from one call to the next: the per-voxel fields, hardening and
+ * orientation state, the macro state, the increment records and the
+ * namelist.  Taken between calls (not while the RVE is in a batch); restored
+ * on the current CUDA device as a new handle that continues exactly as the
+ * original would (bit-identical increments).  A snapshot is read only by the
+ * same build of the library (VOCE_ERR_UNSUPPORTED otherwise); a damaged one
+ * fails with VOCE_ERR_PARSE. */
+long long voce_rve_snapshot_size(voce_rve *r);
+int voce_rve_snapshot(voce_rve *r, void *buf, long long size);
+int voce_rve_restore(const void *buf, long long size, voce_rve **out);
+int voce_rve_save(voce_rve *r, const char *path);
+int voce_rve_load(const char *path, voce_rve **out);
+
 int voce_rve_destroy(voce_rve *r);
 
 /* Device-memory footprint of an RVE of the given grid and precision, in

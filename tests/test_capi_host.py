@@ -91,3 +91,11 @@ def test_footprint_scales_with_grid(voce_lib):
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 420 * nv - 9 * 8 * nspec
     assert capi.footprint((256, 256, 256)) < 40e9
+
+
+def test_restore_rejects_damaged_snapshots(voce_lib):
+    """Header checks run before any device work (no GPU needed)."""
+    import ctypes as C
+    h = C.c_void_p()
+    for blob, code in ((b"", 3), (b"x" * 64, 3), (b"VOCESNAP" + bytes(56), 6)):
+        assert voce_lib.voce_rve_restore(blob, len(blob), C.byref(h)) == code

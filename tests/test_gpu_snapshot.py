@@ -1,0 +1,80 @@
+"""RVE snapshot / restore (include/voce_gpu.h): a restored handle continues
+exactly as the original, bit for bit, in every precision form, from memory
+and from a file, alone and inside a batch."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from voce_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed, n=16, grains=12):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = synth.small_case(n, grains, seed, n_steps=6, load=synth.random_traceless_load(rng))
+    return c.write(tempfile.mkdtemp(prefix="snap_"))
+
+
+def _state(r, ks):
+    return ([r.increment(k) for k in ks], r.field("sig_voigt"), r.field("edot_voigt"),
+            r.field("crss"), r.field("tranmat"), r.field("disgrad"), r.field("gammatotal"))
+
+
+def _same(a, b):
+    ia, *fa = a
+    ib, *fb = b
+    assert ia == ib
+    for x, y in zip(fa, fb):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32])
+def test_restore_continues_bit_for_bit(prec, voce_lib):
+    nl = _case(71)
+    with capi.Rve.from_files(nl, prec) as r:
+        r.run(2)
+        blob = r.snapshot()
+        r.run(2)
+        want = _state(r, range(4))
+    with capi.Rve.restore(blob) as r2:
+        assert r2.increments_done == 2
+        r2.run(2)
+        _same(_state(r2, range(4)), want)
+
+
+def test_save_load_file_and_join_batch(voce_lib):
+    nl = _case(72, n=12, grains=8)
+    nl2 = _case(73, n=8, grains=5)
+    path = os.path.join(tempfile.mkdtemp(prefix="snapf_"), "rve.snap")
+    with capi.Rve.from_files(nl) as r:
+        r.run(1)
+        r.save(path)
+        r.run(3)
+        want = _state(r, range(4))
+    # the restored RVE finishes its increments inside a batch with another RVE
+    r2 = capi.Rve.restore_file(path)
+    other = capi.Rve.from_files(nl2)
+    with capi.Batch(capi.PREC_FP64) as b:
+        b.add(r2, 3)
+        b.add(other, 2)
+        assert b.run() == 0
+    _same(_state(r2, range(4)), want)
+    r2.close()
+    other.close()
+
+
+def test_snapshot_refused_inside_a_batch_and_damaged_blobs(voce_lib):
+    nl = _case(74, n=8, grains=4)
+    with capi.Rve.from_files(nl) as r, capi.Batch(capi.PREC_FP64) as b:
+        b.add(r, 1)
+        with pytest.raises(capi.VoceError) as ei:
+            r.snapshot()
+        assert ei.value.code == 9
+        b.remove(r)
+        blob = r.snapshot()
+    with pytest.raises(capi.VoceError) as ei:
+        capi.Rve.restore(blob[:-8])
+    assert ei.value.code == 3

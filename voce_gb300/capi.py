@@ -147,6 +147,11 @@ PROTOTYPES = [
     ("voce_batch_get_kernel_time", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                             C.POINTER(C.c_longlong)]),
     ("voce_batch_reset_kernel_times", C.c_int, [C.c_void_p]),
+    ("voce_rve_snapshot_size", C.c_longlong, [C.c_void_p]),
+    ("voce_rve_snapshot", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("voce_rve_restore", C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_void_p)]),
+    ("voce_rve_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("voce_rve_load", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -373,6 +378,37 @@ class Rve:
         finally:
             libc.fclose(vm)
             libc.fclose(err)
+
+    def snapshot(self) -> bytes:
+        """The RVE's whole state as bytes (voce_rve_snapshot)."""
+        n = load().voce_rve_snapshot_size(self._h)
+        if n < 0:
+            _check(-n)
+        buf = C.create_string_buffer(n)
+        _check(load().voce_rve_snapshot(self._h, buf, n))
+        return buf.raw
+
+    @classmethod
+    def restore(cls, blob: bytes) -> "Rve":
+        h = C.c_void_p()
+        _check(load().voce_rve_restore(blob, len(blob), C.byref(h)))
+        r = cls(h, (0, 0, 0))
+        r.dims = tuple(r.namelist().CellDim)
+        r.nv = int(np.prod(r.dims))
+        return r
+
+    def save(self, path: str) -> None:
+        _check(load().voce_rve_save(self._h, path.encode()))
+
+    @classmethod
+    def restore_file(cls, path: str) -> "Rve":
+        """A handle from a file written by save (voce_rve_load)."""
+        h = C.c_void_p()
+        _check(load().voce_rve_load(path.encode(), C.byref(h)))
+        r = cls(h, (0, 0, 0))
+        r.dims = tuple(r.namelist().CellDim)
+        r.nv = int(np.prod(r.dims))
+        return r
 
     def close(self) -> None:
         if self._h:

@@ -15,6 +15,8 @@
 #include <cstdlib>
 #include <algorithm>
 #include <cstring>
+#include <cstddef>
+#include <cstdint>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -46,6 +48,12 @@ int voce::set_error(int code, const char *msg)
 }
 
 namespace {
+
+#define CUDA_TRY_NEG(x)                                                                    \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess) return -fail(VOCE_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
 
 #define CUDA_TRY(x)                                                                        \
     do {                                                                                   \
@@ -408,6 +416,84 @@ int voce_mesh_read(const char *path, const int dims[3], double *eul, int *grain,
     return VOCE_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device arrays of one RVE, state and scratch, sized from its descriptor;
+// the twiddle tables are filled, the rest is left to the caller.
+int alloc_device(voce_rve *r)
+{
+    RveDesc &d = r->d;
+    const long long nv = d.nv;
+    int rc = VOCE_OK;
+#define AL(ptr, n) if ((rc = dalloc(r, ptr, (size_t)(n))) != VOCE_OK) return rc;
+    AL(d.sig, 6 * nv); AL(d.sigp, 6 * nv); AL(d.eps, 5 * nv); AL(d.dgs, 6 * nv); AL(d.dga, 3 * nv);
+    AL(d.tm, 9 * nv); AL(d.sch, 60 * nv); AL(d.sg, 21 * nv); AL(d.crss, 24 * nv); AL(d.itau, 24 * nv);
+    AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
+    AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.diag, 3 * nv); AL(d.phase, nv);
+    d.sch32 = nullptr;
+    d.itau32 = nullptr;
+    d.sgp32 = nullptr;
+    if (d.nr32) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
+    AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
+    AL(d.macro, 1);
+    d.incr_cap = 32;   // increments per host read-back
+    AL(d.itlog, (size_t)d.incr_cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
+    AL(d.incr, d.incr_cap);
+    const size_t csz = d.mixed ? sizeof(float2) : sizeof(double2);
+    char *p;
+    AL(p, 6 * d.nspec * csz); d.spec = p;
+    AL(p, 3 * d.nspec * csz); d.aacc = p;
+    const int Ls[3] = {d.nx, d.ny, d.nz};
+    const void **tws[3] = {&d.twx, &d.twy, &d.twz};
+    for (int a = 0; a < 3; ++a) {
+        AL(p, (size_t)Ls[a] * csz);
+        if (d.mixed) {
+            auto t = twiddles<float2, float>(Ls[a]);
+            CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
+        } else {
+            auto t = twiddles<double2, double>(Ls[a]);
+            CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        }
+        *tws[a] = p;
+    }
+#undef AL
+    CUDA_TRY(cudaMallocHost(&r->h_flag, 64));
+    return VOCE_OK;
+}
+
+// The device arrays that carry an RVE's state from one call to the next, in
+// snapshot order, with their sizes in bytes: f(&pointer, bytes).
+template <class F>
+void for_state(RveDesc &d, F &&f)
+{
+    const size_t nv = (size_t)d.nv, D = sizeof(double), S = sizeof(float);
+    f((void **)&d.sig, 6 * nv * D);      f((void **)&d.sigp, 6 * nv * D);
+    f((void **)&d.eps, 5 * nv * D);      f((void **)&d.dgs, 6 * nv * D);
+    f((void **)&d.dga, 3 * nv * D);      f((void **)&d.tm, 9 * nv * D);
+    f((void **)&d.sch, 60 * nv * D);     f((void **)&d.sg, 21 * nv * D);
+    f((void **)&d.crss, 24 * nv * D);    f((void **)&d.itau, 24 * nv * D);
+    f((void **)&d.gamacum, nv * D);      f((void **)&d.gtot, 12 * nv * D);
+    f((void **)&d.edot, 5 * nv * D);     f((void **)&d.gamdot, 12 * nv * D);
+    f((void **)&d.taux, 12 * nv * D);    f((void **)&d.svm, nv * D);
+    f((void **)&d.evm, nv * D);          f((void **)&d.rotl, 3 * nv * D);
+    f((void **)&d.diag, 3 * nv * D);     f((void **)&d.phase, nv * sizeof(int));
+    if (d.nr32) {
+        f((void **)&d.sch32, 60 * nv * S);
+        f((void **)&d.itau32, 24 * nv * S);
+        f((void **)&d.sgp32, 21 * nv * S);
+    }
+    // the antisymmetric Green update summed over the current increment's
+    // iterations, and the macro state
+    f((void **)&d.aacc, 3 * (size_t)d.nspec * (d.mixed ? sizeof(float2) : sizeof(double2)));
+    f((void **)&d.macro, sizeof(MacroDev));
+}
+
+}  // namespace
+
+extern "C" {
+
 long long voce_rve_footprint(const int dims[3], int precision)
 {
     const long long nv = (long long)dims[0] * dims[1] * dims[2];
@@ -589,46 +675,12 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(d.nr32 != 0));
     r->npart = (int)(nb < cap ? nb : cap);
     d.npart = r->npart;
-    int rc = VOCE_OK;
-#define AL(ptr, n) if ((rc = dalloc(r, ptr, (size_t)(n))) != VOCE_OK) { delete r; return rc; }
-    AL(d.sig, 6 * nv); AL(d.sigp, 6 * nv); AL(d.eps, 5 * nv); AL(d.dgs, 6 * nv); AL(d.dga, 3 * nv);
-    AL(d.tm, 9 * nv); AL(d.sch, 60 * nv); AL(d.sg, 21 * nv); AL(d.crss, 24 * nv); AL(d.itau, 24 * nv);
-    AL(d.gamacum, nv); AL(d.gtot, 12 * nv); AL(d.edot, 5 * nv); AL(d.gamdot, 12 * nv); AL(d.taux, 12 * nv);
-    AL(d.svm, nv); AL(d.evm, nv); AL(d.rotl, 3 * nv); AL(d.diag, 3 * nv); AL(d.phase, nv);
-    d.sch32 = nullptr;
-    d.itau32 = nullptr;
-    d.sgp32 = nullptr;
-    if (d.nr32) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
-    AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
-    AL(d.macro, 1);
-    d.incr_cap = 32;   // increments per host read-back
-    AL(d.itlog, (size_t)d.incr_cap * VOCE_ITLOG * (d.iter_max > 0 ? d.iter_max : 1));
-    AL(d.incr, d.incr_cap);
-    const size_t csz = d.mixed ? sizeof(float2) : sizeof(double2);
-    {
-        char *p;
-        AL(p, 6 * d.nspec * csz); d.spec = p;
-        AL(p, 3 * d.nspec * csz); d.aacc = p;
-        const int Ls[3] = {nx, ny, nz};
-        const void **tws[3] = {&d.twx, &d.twy, &d.twz};
-        for (int a = 0; a < 3; ++a) {
-            AL(p, (size_t)Ls[a] * csz);
-            if (r->precision) {
-                auto t = twiddles<float2, float>(Ls[a]);
-                CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
-            } else {
-                auto t = twiddles<double2, double>(Ls[a]);
-                CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(double2), cudaMemcpyHostToDevice));
-            }
-            *tws[a] = p;
-        }
-    }
+    int rc = alloc_device(r);
+    if (rc) { delete r; return rc; }
     double *d_eul = nullptr;
-    AL(d_eul, 3 * nv);
-#undef AL
+    if ((rc = dalloc(r, d_eul, (size_t)(3 * nv))) != VOCE_OK) { delete r; return rc; }
     CUDA_TRY(cudaMemcpyAsync(d_eul, mesh->euler_deg, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(d.phase, mesh->phase, sizeof(int) * nv, cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMallocHost(&r->h_flag, 64));
     r->nl = *nl;
     r->phase.assign(mesh->phase, mesh->phase + nv);
     if (mesh->grain) r->grain.assign(mesh->grain, mesh->grain + nv);
@@ -1117,6 +1169,203 @@ int voce_rve_get_namelist(const voce_rve *r, voce_namelist *out)
     if (!r || !out) return fail(VOCE_ERR_ARG, "null argument");
     *out = r->nl;
     return VOCE_OK;
+}
+
+}  // extern "C"
+
+// ---- snapshot / restore ----------------------------------------------------
+namespace {
+
+struct SnapHead {
+    char magic[8];
+    uint32_t version, desc_size, macro_size, nl_size, incr_size;
+    int32_t precision, npart, n_incr, pad;
+    int64_t nv, total;
+};
+const char kSnapMagic[8] = {'V', 'O', 'C', 'E', 'S', 'N', 'A', 'P'};
+
+// Writes (or, with out == nullptr, only sizes) the snapshot of r.
+long long snapshot_write(voce_rve *r, char *out)
+{
+    RveDesc &d = r->d;
+    long long pos = 0;
+    auto put = [&](const void *src, size_t n) {
+        if (out) std::memcpy(out + pos, src, n);
+        pos += (long long)n;
+    };
+    SnapHead h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kSnapMagic, 8);
+    h.version = 1;
+    h.desc_size = sizeof(RveDesc);
+    h.macro_size = sizeof(MacroDev);
+    h.nl_size = sizeof(voce_namelist);
+    h.incr_size = sizeof(voce_increment);
+    h.precision = r->precision;
+    h.npart = r->npart;
+    h.n_incr = (int32_t)r->incr.size();
+    h.nv = d.nv;
+    put(&h, sizeof(h));
+    put(&d, sizeof(RveDesc));
+    put(&r->nl, sizeof(voce_namelist));
+    put(r->grain.data(), sizeof(int) * r->grain.size());
+    put(r->phase.data(), sizeof(int) * r->phase.size());
+    for (size_t k = 0; k < r->incr.size(); ++k) {
+        put(&r->incr[k], sizeof(voce_increment));
+        const int64_t n = (int64_t)r->itlog[k].size();
+        put(&n, sizeof(n));
+        put(r->itlog[k].data(), sizeof(double) * (size_t)n);
+    }
+    int rc = VOCE_OK;
+    for_state(d, [&](void **p, size_t n) {
+        if (out && rc == VOCE_OK) {
+            cudaError_t e = cudaMemcpy(out + pos, *p, n, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "snapshot copy: %s", cudaGetErrorString(e));
+        }
+        pos += (long long)n;
+    });
+    if (rc) return -rc;
+    if (out) {
+        h.total = pos;
+        std::memcpy(out + offsetof(SnapHead, total), &h.total, sizeof(h.total));
+    }
+    return pos;
+}
+
+}  // namespace
+
+extern "C" {
+
+long long voce_rve_snapshot_size(voce_rve *r)
+{
+    if (!r) return -fail(VOCE_ERR_ARG, "null argument");
+    if (!r->batch) {
+        CUDA_TRY_NEG(cudaStreamSynchronize(r->stream));
+        const int rc = collect_new(r, false);
+        if (rc) return -rc;
+    }
+    return snapshot_write(r, nullptr);
+}
+
+int voce_rve_snapshot(voce_rve *r, void *buf, long long size)
+{
+    if (!r || !buf) return fail(VOCE_ERR_ARG, "null argument");
+    if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch; remove it first");
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    int rc = collect_new(r, false);
+    if (rc) return rc;
+    const long long need = snapshot_write(r, nullptr);
+    if (size < need) return fail(VOCE_ERR_ARG, "snapshot buffer of %lld bytes, %lld needed", size, need);
+    const long long n = snapshot_write(r, static_cast<char *>(buf));
+    return n < 0 ? (int)-n : VOCE_OK;
+}
+
+int voce_rve_restore(const void *buf, long long size, voce_rve **out)
+{
+    if (!buf || !out) return fail(VOCE_ERR_ARG, "null argument");
+    const char *in = static_cast<const char *>(buf);
+    SnapHead h;
+    if (size < (long long)sizeof(h)) return fail(VOCE_ERR_PARSE, "snapshot too short");
+    std::memcpy(&h, in, sizeof(h));
+    if (std::memcmp(h.magic, kSnapMagic, 8) != 0) return fail(VOCE_ERR_PARSE, "not an RVE snapshot");
+    if (h.version != 1 || h.desc_size != sizeof(RveDesc) || h.macro_size != sizeof(MacroDev) ||
+        h.nl_size != sizeof(voce_namelist) || h.incr_size != sizeof(voce_increment))
+        return fail(VOCE_ERR_UNSUPPORTED, "snapshot written by a different build of the library");
+    if (h.total != size) return fail(VOCE_ERR_PARSE, "snapshot of %lld bytes, header says %lld", size, (long long)h.total);
+    long long pos = sizeof(h);
+    auto get = [&](void *dst, size_t n) -> bool {
+        if (pos + (long long)n > size) return false;
+        std::memcpy(dst, in + pos, n);
+        pos += (long long)n;
+        return true;
+    };
+    voce_rve *r = new voce_rve();
+    RveDesc &d = r->d;
+    bool ok = get(&d, sizeof(RveDesc)) && get(&r->nl, sizeof(voce_namelist));
+    if (!ok || d.nv != h.nv || h.npart < 1 || h.n_incr < 0) {
+        delete r;
+        return fail(VOCE_ERR_PARSE, "snapshot header and descriptor disagree");
+    }
+    r->precision = h.precision;
+    r->npart = h.npart;
+    r->grain.resize((size_t)d.nv);
+    r->phase.resize((size_t)d.nv);
+    ok = get(r->grain.data(), sizeof(int) * (size_t)d.nv) && get(r->phase.data(), sizeof(int) * (size_t)d.nv);
+    for (int k = 0; ok && k < h.n_incr; ++k) {
+        voce_increment rec;
+        int64_t n = 0;
+        ok = get(&rec, sizeof(rec)) && get(&n, sizeof(n)) && n >= 0 && n < (int64_t)1 << 30;
+        if (!ok) break;
+        std::vector<double> lg((size_t)n);
+        ok = get(lg.data(), sizeof(double) * (size_t)n);
+        r->incr.push_back(rec);
+        r->itlog.push_back(std::move(lg));
+    }
+    if (!ok) {
+        delete r;
+        return fail(VOCE_ERR_PARSE, "truncated snapshot");
+    }
+    r->n_done = h.n_incr;
+    r->n_steps = r->nl.N_steps;
+    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete r;
+        return fail(VOCE_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    int rc = alloc_device(r);
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    for_state(d, [&](void **p, size_t n) {
+        if (rc) return;
+        if (pos + (long long)n > size) { rc = fail(VOCE_ERR_PARSE, "truncated snapshot"); return; }
+        cudaError_t e2 = cudaMemcpy(*p, in + pos, n, cudaMemcpyHostToDevice);
+        if (e2 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore copy: %s", cudaGetErrorString(e2));
+        pos += (long long)n;
+    });
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    // the device record rings start empty; the next increment writes slot
+    // (istep - 1) mod capacity as usual
+    *out = r;
+    return VOCE_OK;
+}
+
+int voce_rve_save(voce_rve *r, const char *path)
+{
+    if (!r || !path) return fail(VOCE_ERR_ARG, "null argument");
+    const long long n = voce_rve_snapshot_size(r);
+    if (n < 0) return (int)-n;
+    std::vector<char> buf((size_t)n);
+    int rc = voce_rve_snapshot(r, buf.data(), n);
+    if (rc) return rc;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(VOCE_ERR_IO, "cannot open %s", path);
+    const bool ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    if (std::fclose(f) != 0 || !ok) return fail(VOCE_ERR_IO, "cannot write %s", path);
+    return VOCE_OK;
+}
+
+int voce_rve_load(const char *path, voce_rve **out)
+{
+    if (!path || !out) return fail(VOCE_ERR_ARG, "null argument");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(VOCE_ERR_IO, "cannot open %s", path);
+    std::fseek(f, 0, SEEK_END);
+    const long n = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (n <= 0) {
+        std::fclose(f);
+        return fail(VOCE_ERR_IO, "cannot read %s", path);
+    }
+    std::vector<char> buf((size_t)n);
+    const bool ok = std::fread(buf.data(), 1, buf.size(), f) == buf.size();
+    std::fclose(f);
+    if (!ok) return fail(VOCE_ERR_IO, "cannot read %s", path);
+    return voce_rve_restore(buf.data(), (long long)n, out);
 }
 
 int voce_rve_destroy(voce_rve *r)
