@@ -423,7 +423,9 @@ def run_cfg3(args):
     from voce_gb300 import capi, synth
     chosen = args.precision or "mixed_nr32"
     t0 = time.perf_counter()
-    case = synth.config3(n_steps=250)
+    # config 3 (synth.config3), its mesh tessellated on the GPU
+    case = synth.Case("cfg3_256", _voronoi_mesh(256, 4096, 3), synth.CU_LIKE,
+                      synth.plane_strain_compression(), 0.2, 250)
     t_mesh = time.perf_counter() - t0
     d = tempfile.mkdtemp(prefix="cfg3_")
     synth.write_sx(os.path.join(d, "mat.sx"), case.mat)
@@ -480,6 +482,18 @@ def run_cfg3(args):
     print(json.dumps(res), flush=True)
 
 
+def _voronoi_mesh(n, n_grains, seed):
+    """synth.voronoi_mesh(n, n_grains, seed), with the tessellation computed on
+    the GPU (voce_mesh_voronoi; the same mesh, tests/test_gpu_voronoi.py)."""
+    import numpy as np
+    from voce_gb300 import capi, synth
+    rng = np.random.Generator(np.random.PCG64(seed))
+    seeds = rng.random((n_grains, 3))
+    eul_g = synth.so3_uniform_bunge(rng, n_grains)
+    eul, grain, phase = capi.mesh_voronoi((n, n, n), seeds, eul_g)
+    return synth.Mesh((n, n, n), eul, grain, phase)
+
+
 def _loguniform_int(rng, lo, hi):
     import math
     return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
@@ -533,7 +547,7 @@ def run_cfg4(args):
         edge = int(rng.choice([16, 32, 48, 64]))
         grains = _loguniform_int(rng, 8, 512)
         load = synth.random_traceless_load(rng)
-        mesh = synth.voronoi_mesh(edge, grains, 10000 + i)
+        mesh = _voronoi_mesh(edge, grains, 10000 + i)
         cases.append(synth.Case("b%d" % i, mesh, synth.CU_LIKE, load, 0.25, 40))
     t_gen = time.perf_counter() - t0
     nv_tot = sum(c.mesh.nvox for c in cases)
@@ -651,7 +665,7 @@ def run_cfg5(args):
         grains = _loguniform_int(rng, 8, 2048)
         load = synth.random_traceless_load(rng)
         inc = max(1, int(round(args.inc_scale * rng.integers(10, 81))))
-        mesh = synth.voronoi_mesh(edge, min(grains, edge ** 3), 20000 + i)
+        mesh = _voronoi_mesh(edge, min(grains, edge ** 3), 20000 + i)
         c = synth.Case("q%d" % i, mesh, synth.CU_LIKE, load, 0.2, inc)
         nl, sx = _rve_inputs(c, d, str(i))
         reqs.append((t_arr, c, nl, sx, inc))

@@ -201,6 +201,17 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out);
 #define VOCE_NOALLOC_MAX_DOUBLES 4194304
 int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out);
 
+/* Synthetic microstructure on the GPU (no counterpart in the reference,
+ * whose microstructure comes from a mesh file): the periodic Voronoi
+ * tessellation of the unit cube by n_seeds seeds (x, y, z in [0,1)) on a
+ * dims[0] x dims[1] x dims[2] grid of voxel centres ((i + 0.5) / n), by
+ * minimum-image distance in FP64, ties to the lowest seed.  Fills a mesh
+ * ready for voce_rve_create: grain = seed index + 1, phase = 1, and the
+ * Bunge angles (degrees) given for its grain.  A request can carry seeds and
+ * grain orientations instead of a whole mesh file. */
+int voce_mesh_voronoi(const int dims[3], int n_seeds, const double *seeds_xyz,
+                      const double *grain_euler_deg, double *euler_deg, int *grain, int *phase);
+
 /* Snapshot / restore (no counterpart in the reference, which has no resume:
  * its io.c dumps are write-only).  A snapshot holds everything an RVE
  * carries from one call to the next: the per-voxel fields, hardening and

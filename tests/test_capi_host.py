@@ -99,3 +99,55 @@ def test_restore_rejects_damaged_snapshots(voce_lib):
     h = C.c_void_p()
     for blob, code in ((b"", 3), (b"x" * 64, 3), (b"VOCESNAP" + bytes(56), 6)):
         assert voce_lib.voce_rve_restore(blob, len(blob), C.byref(h)) == code
+
+
+def test_mesh_reader_parses_like_strtod_on_every_format(voce_lib):
+    """The parallel mesh reader (more than 1 MiB: several chunks) gives the
+    doubles the C library's conversion gives (Python's float() is correctly
+    rounded, as glibc's strtod is), for every number format a mesh file may
+    hold: fixed with up to 22 fraction digits, more than 15 significant
+    digits, exponents, signs, negative zero; blanks, tabs, CRLF and blank
+    lines between records."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    dims = (40, 40, 40)
+    nv = 40 ** 3
+    fmts = ["%.6f", "%.17g", "%.3e", "%+.9f", "%.22f", "%.0f", "%.20g"]
+    lines, want = [], np.zeros((nv, 3))
+    v = 0
+    for i in range(40):
+        for j in range(40):
+            for k in range(40):
+                toks = []
+                for q in range(3):
+                    x = float(rng.uniform(-400, 400)) * (10.0 ** int(rng.integers(-3, 4)))
+                    if v % 997 == 0 and q == 0:
+                        x = -0.0
+                    t = fmts[(v + q) % len(fmts)] % x
+                    toks.append(t)
+                    want[v, q] = float(t)
+                sep = "\t" if v % 3 == 0 else " "
+                end = "\r\n" if v % 5 == 0 else "\n"
+                lines.append(sep.join(toks) + " %d %d +%d %d %d" % (i + 1, j + 1, k + 1, v % 7 + 1, 1) + end)
+                if v % 4999 == 0:
+                    lines.append("   \n")
+                v += 1
+    d = tempfile.mkdtemp(prefix="meshfmt_")
+    path = os.path.join(d, "mesh.txt")
+    with open(path, "w", newline="") as f:
+        f.write("".join(lines))
+    assert os.path.getsize(path) > (1 << 20)
+    eul, grain, phase = capi.read_mesh(path, dims)
+    got = np.asarray(eul).reshape(nv, 3)
+    assert got.tobytes() == want.tobytes()
+    assert np.array_equal(grain, np.arange(nv) % 7 + 1) and (phase == 1).all()
+    # a record out of place is still caught in a later chunk
+    bad = list(lines)
+    idx = len(bad) * 3 // 4
+    bad[idx] = bad[idx].replace("\t", " ").split(" ")
+    bad[idx][3] = "999"
+    bad[idx] = " ".join(bad[idx])
+    with open(path, "w", newline="") as f:
+        f.write("".join(bad))
+    with pytest.raises(capi.VoceError) as ei:
+        capi.read_mesh(path, dims)
+    assert ei.value.code == 3

@@ -26,7 +26,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 # extra nvcc flags (e.g. -DVOCE_NR_MIXED_BLOCKS=3) for tuning builds
 NVFLAGS += os.environ.get("VOCE_NVCC_EXTRA", "").split()
-SOURCES = ["voce_kernels.cu", "voce_api.cu", "voce_server.cpp", "voce_io.cpp"]
+SOURCES = ["voce_kernels.cu", "voce_api.cu", "voce_server.cpp", "voce_io.cpp", "voce_parse.cpp"]
 LEGACY = os.path.join(CSRC, "legacy")
 LEGACY_SOURCES = ["voce_legacy.cpp", "voce_legacy_cxx.cpp"]
 LEGACY_LIB = os.path.join(LIBDIR, "libvoce_legacy.so")

@@ -152,6 +152,9 @@ PROTOTYPES = [
     ("voce_rve_restore", C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_void_p)]),
     ("voce_rve_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("voce_rve_load", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("voce_mesh_voronoi", C.c_int, [C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -205,6 +208,20 @@ def read_slip(path: str) -> VoceSlip:
     s = VoceSlip()
     _check(load().voce_slip_read(path.encode(), C.byref(s)))
     return s
+
+
+def mesh_voronoi(dims: Sequence[int], seeds: np.ndarray, grain_euler_deg: np.ndarray):
+    """voce_mesh_voronoi: (euler (nv, 3), grain, phase) of the periodic Voronoi
+    tessellation of the grid by `seeds` (n, 3), computed on the GPU."""
+    nv = int(np.prod(dims))
+    s = np.ascontiguousarray(seeds, dtype=np.float64)
+    ge = np.ascontiguousarray(grain_euler_deg, dtype=np.float64)
+    eul = np.zeros((nv, 3))
+    grain = np.zeros(nv, dtype=np.int32)
+    phase = np.zeros(nv, dtype=np.int32)
+    d = (C.c_int * 3)(*dims)
+    _check(load().voce_mesh_voronoi(d, len(s), _dptr(s), _dptr(ge), _dptr(eul), _iptr(grain), _iptr(phase)))
+    return eul, grain, phase
 
 
 def read_mesh(path: str, dims: Sequence[int]):

@@ -376,45 +376,7 @@ int voce_slip_read(const char *path, voce_slip *out)
 
 // InitMicroStruct's reader (init.c:410-433): one line per voxel
 // "phi1 Phi phi2 i j k grain phase", x slowest / z fastest, 1-based.
-int voce_mesh_read(const char *path, const int dims[3], double *eul, int *grain, int *phase)
-{
-    if (!path || !dims || !eul || !grain || !phase) return fail(VOCE_ERR_ARG, "null argument");
-    FILE *fp = std::fopen(path, "rb");
-    if (!fp) return fail(VOCE_ERR_IO, "cannot open mesh '%s'", path);
-    std::fseek(fp, 0, SEEK_END);
-    long sz = std::ftell(fp);
-    std::fseek(fp, 0, SEEK_SET);
-    std::vector<char> txt((size_t)sz + 1);
-    size_t got = std::fread(txt.data(), 1, (size_t)sz, fp);
-    std::fclose(fp);
-    txt[got] = 0;
-    const long long nv = (long long)dims[0] * dims[1] * dims[2];
-    char *p = txt.data();
-    for (long long v = 0; v < nv; ++v) {
-        char *e;
-        double a[3];
-        long iv[5];
-        for (int q = 0; q < 3; ++q) {
-            a[q] = std::strtod(p, &e);
-            if (e == p) return fail(VOCE_ERR_PARSE, "mesh '%s': short line at voxel %lld", path, v);
-            p = e;
-        }
-        for (int q = 0; q < 5; ++q) {
-            iv[q] = std::strtol(p, &e, 10);
-            if (e == p) return fail(VOCE_ERR_PARSE, "mesh '%s': short line at voxel %lld", path, v);
-            p = e;
-        }
-        while (*p && *p != '\n') ++p;
-        if (*p) ++p;
-        long long idx = ((iv[0] - 1) * (long long)dims[1] + iv[1] - 1) * dims[2] + iv[2] - 1;
-        if (idx != v)
-            return fail(VOCE_ERR_PARSE, "mesh '%s': inconsistent index system at voxel %lld", path, v);
-        eul[3 * v] = a[0]; eul[3 * v + 1] = a[1]; eul[3 * v + 2] = a[2];
-        grain[v] = (int)iv[3];
-        phase[v] = (int)iv[4];
-    }
-    return VOCE_OK;
-}
+// voce_mesh_read: voce_parse.cpp
 
 }  // extern "C"
 
@@ -1366,6 +1328,50 @@ int voce_rve_load(const char *path, voce_rve **out)
     std::fclose(f);
     if (!ok) return fail(VOCE_ERR_IO, "cannot read %s", path);
     return voce_rve_restore(buf.data(), (long long)n, out);
+}
+
+int voce_mesh_voronoi(const int dims[3], int n_seeds, const double *seeds_xyz,
+                      const double *grain_euler_deg, double *euler_deg, int *grain, int *phase)
+{
+    if (!dims || !seeds_xyz || !grain_euler_deg || !euler_deg || !grain || !phase)
+        return fail(VOCE_ERR_ARG, "null argument");
+    if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || n_seeds < 1)
+        return fail(VOCE_ERR_ARG, "empty grid or no seeds");
+    const long long nv = (long long)dims[0] * dims[1] * dims[2];
+    if (nv > (1LL << 31) - 1) return fail(VOCE_ERR_UNSUPPORTED, "grid of %lld voxels", nv);
+    double *d_seeds = nullptr;
+    int *d_label = nullptr;
+    cudaStream_t s = nullptr;
+    int rc = VOCE_OK;
+    std::vector<int> lab((size_t)nv);
+    do {
+        cudaError_t e;
+        if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaMalloc(&d_seeds, sizeof(double) * 3 * (size_t)n_seeds)) != cudaSuccess ||
+            (e = cudaMalloc(&d_label, sizeof(int) * (size_t)nv)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(d_seeds, seeds_xyz, sizeof(double) * 3 * (size_t)n_seeds,
+                                 cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = launch_voronoi(dims[0], dims[1], dims[2], n_seeds, d_seeds, d_label, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(lab.data(), d_label, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost, s)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+            rc = fail(e == cudaErrorMemoryAllocation ? VOCE_ERR_NOMEM : VOCE_ERR_CUDA, "voronoi: %s",
+                      cudaGetErrorString(e));
+        }
+    } while (0);
+    if (d_seeds) cudaFree(d_seeds);
+    if (d_label) cudaFree(d_label);
+    if (s) cudaStreamDestroy(s);
+    if (rc) return rc;
+    for (long long v = 0; v < nv; ++v) {
+        const int g = lab[(size_t)v];
+        euler_deg[3 * v] = grain_euler_deg[3 * g];
+        euler_deg[3 * v + 1] = grain_euler_deg[3 * g + 1];
+        euler_deg[3 * v + 2] = grain_euler_deg[3 * g + 2];
+        grain[v] = g + 1;
+        phase[v] = 1;
+    }
+    return VOCE_OK;
 }
 
 int voce_rve_destroy(voce_rve *r)

@@ -1682,6 +1682,57 @@ cudaError_t launch_batch_tick_timed(const BatchPlan &bp, cudaStream_t s, Prof &p
     return cudaGetLastError();
 }
 
+// Periodic Voronoi labels: each voxel centre ((x+0.5)/nx, ...) of the unit
+// cube takes the nearest seed by minimum-image distance, ties to the lowest
+// index.  The arithmetic is that of the host generator's numpy form: the
+// image by round-half-to-even (rint), the squared distance summed as
+// (d0^2 + d1^2) + d2^2 without contraction, strict < over seeds in order.
+__global__ void k_voronoi(int nx, int ny, int nz, int ns, const double *__restrict__ seeds,
+                          int *__restrict__ label)
+{
+    extern __shared__ double s_seed[];   // 3 x VORONOI_TILE
+    const long long nv = (long long)nx * ny * nz;
+    const long long v0 = (long long)blockIdx.x * blockDim.x;
+    const long long v = v0 + threadIdx.x;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (v < nv) {
+        const int z = (int)(v % nz), y = (int)((v / nz) % ny), x = (int)(v / ((long long)ny * nz));
+        p0 = ((double)x + 0.5) / (double)nx;
+        p1 = ((double)y + 0.5) / (double)ny;
+        p2 = ((double)z + 0.5) / (double)nz;
+    }
+    double best = 1e300;
+    int bi = 0;
+    for (int t0 = 0; t0 < ns; t0 += VORONOI_TILE) {
+        const int tn = min(VORONOI_TILE, ns - t0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * tn; i += blockDim.x) s_seed[i] = seeds[3 * t0 + i];
+        __syncthreads();
+        for (int j = 0; j < tn; ++j) {
+            double d0 = __dsub_rn(p0, s_seed[3 * j]);
+            double d1 = __dsub_rn(p1, s_seed[3 * j + 1]);
+            double d2 = __dsub_rn(p2, s_seed[3 * j + 2]);
+            d0 = __dsub_rn(d0, rint(d0));
+            d1 = __dsub_rn(d1, rint(d1));
+            d2 = __dsub_rn(d2, rint(d2));
+            const double dd = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+            if (dd < best) {
+                best = dd;
+                bi = t0 + j;
+            }
+        }
+    }
+    if (v < nv) label[v] = bi;
+}
+
+cudaError_t launch_voronoi(int nx, int ny, int nz, int ns, const double *seeds, int *label, cudaStream_t s)
+{
+    const long long nv = (long long)nx * ny * nz;
+    const int blocks = (int)((nv + 255) / 256);
+    k_voronoi<<<blocks, 256, 3 * VORONOI_TILE * sizeof(double), s>>>(nx, ny, nz, ns, seeds, label);
+    return cudaGetLastError();
+}
+
 // sgp32 = (float)(S_g + S0) once S0 is known (mixed form)
 __global__ void k_fill_p32(RveDesc d)
 {
