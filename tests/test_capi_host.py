@@ -88,8 +88,9 @@ def test_footprint_scales_with_grid(voce_lib):
     nspec = 33 * 64 * 64
     # the mixed forms hold the spectrum in FP32; the single-precision Newton
     # form also keeps float copies of the Schmid vectors, 1/crss and S_g + S0
-    assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec
-    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 420 * nv - 9 * 8 * nspec
+    # (the FP64 form also stores n and omega of every frequency: 9 doubles)
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec - 9 * 8 * nspec
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 420 * nv - 2 * 9 * 8 * nspec
     assert capi.footprint((256, 256, 256)) < 40e9
 
 

@@ -405,6 +405,8 @@ int alloc_device(voce_rve *r)
     AL(d.incr, d.incr_cap);
     const size_t csz = d.mixed ? sizeof(float2) : sizeof(double2);
     char *p;
+    d.gstore = nullptr;
+    if (!d.mixed) AL(d.gstore, 9 * d.nspec);
     AL(p, 6 * d.nspec * csz); d.spec = p;
     AL(p, 3 * d.nspec * csz); d.aacc = p;
     const int Ls[3] = {d.nx, d.ny, d.nz};
@@ -464,7 +466,9 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // doubles per voxel: sig 6, sigp 6, eps 5, dgs 6, dga 3, tm 9, sch 60,
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
-    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 420 : 0)) + nspec * 9 * cplx;
+    // + the FP64 form's stored Green-operator frequencies, 9 doubles each
+    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 420 : 0)) + nspec * 9 * cplx +
+           (precision == VOCE_PREC_FP64 ? nspec * 9 * 8 : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -684,6 +688,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
                 d.Kqf[a * 6 + m] = (float)v;
             }
     }
+    CUDA_TRY(launch_fill_green(d, r->stream));
     // macro state (InitFields init.c:494-499, 536; Evolution locals)
     MacroDev m;
     std::memset(&m, 0, sizeof(m));
@@ -1286,6 +1291,11 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
         if (e2 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore copy: %s", cudaGetErrorString(e2));
         pos += (long long)n;
     });
+    if (rc == VOCE_OK) {
+        cudaError_t e3 = launch_fill_green(d, r->stream);
+        if (e3 == cudaSuccess) e3 = cudaStreamSynchronize(r->stream);
+        if (e3 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore: %s", cudaGetErrorString(e3));
+    }
     if (rc) {
         delete r;
         return rc;

@@ -113,6 +113,7 @@ struct RveDesc {
     void *spec, *aacc;
     const void *twx, *twy, *twz;  // exp(-2 pi i j / L), complex of the spectrum type
     double *part;        // [npart_blocks][VOCE_NPART]
+    double *gstore;      // FP64 form: per frequency n(3) and omega(6), [9][nspec]
     int npart;
     MacroDev *macro;
     double *itlog;       // [iter_max][VOCE_ITLOG] for the current increment
@@ -437,11 +438,9 @@ template <> struct GreenT<float> { typedef float T; };
 __device__ __forceinline__ double green_rcp(double x) { return rcp_nr(x); }
 __device__ __forceinline__ float green_rcp(float x) { return __frcp_rn(x); }
 
-template <typename R, typename G>
-__device__ __forceinline__ void green_rank1(const G *Kq, const G *nd,
-                                            const R (&sr)[6], const R (&si)[6],
-                                            R (&ur)[6], R (&ui)[6], R (&ar)[3], R (&ai)[3],
-                                            R wgt)
+// omega = (Kq nn)^-1 of unit frequency n: 00, 01, 02, 11, 12, 22
+template <typename G>
+__device__ __forceinline__ void green_omega(const G *Kq, const G *nd, G (&w)[6])
 {
     // acoustic tensor K_ik = C0_ijkl n_j n_l (6 sym comps) = Kq * nn
     G nn[6] = {nd[0] * nd[0], nd[1] * nd[1], nd[2] * nd[2],
@@ -463,8 +462,19 @@ __device__ __forceinline__ void green_rank1(const G *Kq, const G *nd,
     G c22 = K[0] * K[1] - K[5] * K[5];
     G det = K[0] * c00 + K[5] * c01 + K[4] * c02;
     G id = green_rcp(det);
-    R w00 = R(c00 * id), w01 = R(c01 * id), w02 = R(c02 * id);
-    R w11 = R(c11 * id), w12 = R(c12 * id), w22 = R(c22 * id);
+    w[0] = c00 * id; w[1] = c01 * id; w[2] = c02 * id;
+    w[3] = c11 * id; w[4] = c12 * id; w[5] = c22 * id;
+}
+
+// dU -= wgt (omega sig^ n) (x) n, symmetric and antisymmetric parts
+template <typename R, typename G>
+__device__ __forceinline__ void green_update(const G (&w)[6], const G *nd,
+                                             const R (&sr)[6], const R (&si)[6],
+                                             R (&ur)[6], R (&ui)[6], R (&ar)[3], R (&ai)[3],
+                                             R wgt)
+{
+    R w00 = R(w[0]), w01 = R(w[1]), w02 = R(w[2]);
+    R w11 = R(w[3]), w12 = R(w[4]), w22 = R(w[5]);
     R n0 = R(nd[0]), n1 = R(nd[1]), n2 = R(nd[2]);
     // t = sig^ n (sig^ symmetric: 00,11,22,12,02,01)
     R t0r = sr[0] * n0 + sr[5] * n1 + sr[4] * n2, t0i = si[0] * n0 + si[5] * n1 + si[4] * n2;
@@ -487,14 +497,26 @@ __device__ __forceinline__ void green_rank1(const G *Kq, const G *nd,
     ar[2] += hh * (v0r * n1 - v1r * n0);   ai[2] += hh * (v0i * n1 - v1i * n0);
 }
 
+template <typename R, typename G>
+__device__ __forceinline__ void green_rank1(const G *Kq, const G *nd,
+                                            const R (&sr)[6], const R (&si)[6],
+                                            R (&ur)[6], R (&ui)[6], R (&ar)[3], R (&ai)[3],
+                                            R wgt)
+{
+    G w[6];
+    green_omega<G>(Kq, nd, w);
+    green_update<R, G>(w, nd, sr, si, ur, ui, ar, ai, wgt);
+}
+
 __device__ __forceinline__ const double *green_kq(const RveDesc &d, double *) { return d.Kq; }
 __device__ __forceinline__ const float *green_kq(const RveDesc &d, float *) { return d.Kqf; }
 
-// Apply the Green operator at frequency (ix,iy,iz).  In: B-basis stress
-// spectrum (br, bi).  Out: B-basis symmetric update in (br, bi) and the
-// antisymmetric update (ar, ai).
+// Apply the Green operator at frequency (ix,iy,iz), spectral index o.  In:
+// B-basis stress spectrum (br, bi).  Out: B-basis symmetric update in
+// (br, bi) and the antisymmetric update (ar, ai).  With d.gstore (FP64 form)
+// the frequency's n and omega are read, else computed.
 template <typename R>
-__device__ __forceinline__ void green_apply(const RveDesc &d, int ix, int iy, int iz,
+__device__ __forceinline__ void green_apply(const RveDesc &d, int ix, int iy, int iz, long long o,
                                             R (&br)[6], R (&bi)[6], R (&ar)[3], R (&ai)[3])
 {
     R sr[6], si[6], ur[6], ui[6];
@@ -507,16 +529,26 @@ __device__ __forceinline__ void green_apply(const RveDesc &d, int ix, int iy, in
     if ((ix | iy | iz) != 0) {
         typedef typename GreenT<R>::T G;
         const G *kq = green_kq(d, (G *)nullptr);
-        G n[3];
-        unit_freq(d, ix, iy, iz, n);
+        G n[3], w[6];
+        if (sizeof(G) == 8 && d.gstore) {
+            const double *gs = d.gstore + o;
+            const long long ns = d.nspec;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) n[q] = (G)__ldg(gs + q * ns);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) w[q] = (G)__ldg(gs + (3 + q) * ns);
+        } else {
+            unit_freq(d, ix, iy, iz, n);
+            green_omega<G>(kq, n, w);
+        }
         bool nyq = ((d.nx % 2 == 0) && ix == d.nx / 2) || ((d.ny % 2 == 0) && iy == d.ny / 2) ||
                    ((d.nz % 2 == 0) && iz == d.nz / 2);
         if (!nyq) {
-            green_rank1<R, G>(kq, n, sr, si, ur, ui, ar, ai, R(1));
+            green_update<R, G>(w, n, sr, si, ur, ui, ar, ai, R(1));
         } else {
             G n2[3];
             unit_freq(d, (d.nx - ix) % d.nx, (d.ny - iy) % d.ny, (d.nz - iz) % d.nz, n2);
-            green_rank1<R, G>(kq, n, sr, si, ur, ui, ar, ai, R(0.5));
+            green_update<R, G>(w, n, sr, si, ur, ui, ar, ai, R(0.5));
             green_rank1<R, G>(kq, n2, sr, si, ur, ui, ar, ai, R(0.5));
         }
     }

@@ -349,7 +349,7 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
             br[c] = e.x;
             bi[c] = e.y;
         }
-        green_apply<R>(d, x, y0 + yl, kz, br, bi, ar, ai);
+        green_apply<R>(d, x, y0 + yl, kz, kb + (long long)x * ny + yl, br, bi, ar, ai);
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
             C e;
@@ -1730,6 +1730,33 @@ cudaError_t launch_voronoi(int nx, int ny, int nz, int ns, const double *seeds, 
     const long long nv = (long long)nx * ny * nz;
     const int blocks = (int)((nv + 255) / 256);
     k_voronoi<<<blocks, 256, 3 * VORONOI_TILE * sizeof(double), s>>>(nx, ny, nz, ns, seeds, label);
+    return cudaGetLastError();
+}
+
+// gstore: n and omega of every frequency of the half spectrum (FP64 form),
+// with the arithmetic green_apply uses when it computes them
+__global__ void k_fill_green(RveDesc d)
+{
+    const long long ns = d.nspec, plane = (long long)d.nx * d.ny;
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < ns;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(o / plane), ix = (int)((o % plane) / d.ny), iy = (int)(o % d.ny);
+        double n[3] = {0.0, 0.0, 0.0}, w[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if ((ix | iy | iz) != 0) {
+            unit_freq(d, ix, iy, iz, n);
+            green_omega<double>(d.Kq, n, w);
+        }
+        for (int q = 0; q < 3; ++q) d.gstore[q * ns + o] = n[q];
+        for (int q = 0; q < 6; ++q) d.gstore[(3 + q) * ns + o] = w[q];
+    }
+}
+
+cudaError_t launch_fill_green(const RveDesc &d, cudaStream_t s)
+{
+    if (!d.gstore) return cudaSuccess;
+    int blocks = (int)((d.nspec + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_fill_green<<<blocks, 256, 0, s>>>(d);
     return cudaGetLastError();
 }
 

@@ -85,6 +85,8 @@ cudaError_t launch_flush(double *buf, long long n, cudaStream_t s);
 // periodic Voronoi labels of an nx x ny x nz grid (synthetic microstructures)
 #define VORONOI_TILE 1024
 cudaError_t launch_voronoi(int nx, int ny, int nz, int ns, const double *seeds, int *label, cudaStream_t s);
+// the FP64 form's stored Green-operator frequencies, once Kq is set in d
+cudaError_t launch_fill_green(const RveDesc &d, cudaStream_t s);
 // the mixed form's float (S_g + S0), once S0 is set in d
 cudaError_t launch_fill_p32(const RveDesc &d, cudaStream_t s);
 // kb_nr blocks resident on the current GPU (SMs x blocks per SM)
