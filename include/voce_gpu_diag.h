@@ -53,6 +53,18 @@ void voce_host_free(void *p);
 /* FP64 FMA throughput of the current device, TFLOP/s (FMA = 2 flops). */
 double voce_measure_fp64_tflops(void);
 
+/* FFT tile tuning.  voce_rve_create times the forward-pass FFT phases with
+ * a few tile sizes (lines per block) on the new RVE and keeps the fastest,
+ * once per grid shape and spectrum precision per process (results do not
+ * depend on the tile).  voce_set_autotune(0) keeps the fixed-budget choice.
+ * voce_rve_get_tiles: the z-forward, y, x/Green, z-inverse tiles and the two
+ * antisymmetric back-transform tiles of r. */
+int voce_set_autotune(int on);
+int voce_rve_get_tiles(const voce_rve *r, int tiles[6]);
+/* Force the tiles (each divides the dimension it splits: ny, nx, ny, ny, ny,
+ * ny; all phases fit in shared memory); between calls, outside a batch. */
+int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -155,6 +155,9 @@ PROTOTYPES = [
     ("voce_mesh_voronoi", C.c_int, [C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("voce_set_autotune", C.c_int, [C.c_int]),
+    ("voce_rve_get_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -395,6 +398,16 @@ class Rve:
         finally:
             libc.fclose(vm)
             libc.fclose(err)
+
+    def tiles(self) -> list:
+        """FFT tiles (lines per block): z forward, y, x/Green, z inverse, and
+        the two antisymmetric back-transform tiles."""
+        t = (C.c_int * 6)()
+        _check(load().voce_rve_get_tiles(self._h, t))
+        return list(t)
+
+    def set_tiles(self, tiles) -> None:
+        _check(load().voce_rve_set_tiles(self._h, (C.c_int * 6)(*tiles)))
 
     def snapshot(self) -> bytes:
         """The RVE's whole state as bytes (voce_rve_snapshot)."""

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -382,6 +383,9 @@ int voce_slip_read(const char *path, voce_slip *out)
 
 namespace {
 
+int autotune_tiles(voce_rve *r);
+extern int g_autotune;
+
 // Device arrays of one RVE, state and scratch, sized from its descriptor;
 // the twiddle tables are filled, the rest is left to the caller.
 int alloc_device(voce_rve *r)
@@ -721,6 +725,10 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     d.zrows = r->tiles.zrows; d.yxt = r->tiles.yxt; d.xkc = r->tiles.xkc;
     d.xkc3 = r->tiles.xkc3; d.zirows = r->tiles.zirows; d.zirows3 = r->tiles.zirows3;
     CUDA_TRY(cudaStreamSynchronize(r->stream));
+    if (g_autotune) {
+        rc = autotune_tiles(r);
+        if (rc) { delete r; return rc; }
+    }
     *out = r;
     return VOCE_OK;
 }
@@ -760,6 +768,8 @@ int voce_rve_create_from_files(const char *namelist_path, int precision, voce_rv
 // ---------------------------------------------------------------------------
 // Evolution (evolution.c:265-622), n increments at a time
 // ---------------------------------------------------------------------------
+}  // extern "C"
+
 namespace {
 
 // Record of one finished increment, copied from the device rings.
@@ -831,6 +841,122 @@ int ensure_self_plan(voce_rve *r)
     int rc = make_plan(one, r->precision, r->plan_desc, r->plan_maps, r->plan);
     if (rc) return rc;
     r->plan_dirty = false;
+    return VOCE_OK;
+}
+
+// ---- FFT tile tuning --------------------------------------------------------
+// The forward-pass FFT phases (z forward, y, x with the Green operator, z
+// inverse) are timed with each candidate tile on the RVE itself, before its
+// first increment, and the fastest kept.  A tile only changes how many lines
+// a block transforms, never a line's arithmetic, so results do not depend on
+// it.  The choice is cached per grid shape and spectrum precision for the
+// life of the process.  The z-inverse phase updates DisGrad, which is saved
+// and put back; the x phase writes the antisymmetric sum, which the first
+// iteration of an increment overwrites; the spectrum is scratch.
+struct TileKey {
+    int nx, ny, nz, mixed;
+    bool operator<(const TileKey &o) const
+    {
+        if (nx != o.nx) return nx < o.nx;
+        if (ny != o.ny) return ny < o.ny;
+        if (nz != o.nz) return nz < o.nz;
+        return mixed < o.mixed;
+    }
+};
+std::mutex g_tile_mu;
+std::map<TileKey, Tiles> g_tile_cache;
+int g_autotune = 1;
+
+void apply_tiles(voce_rve *r, const Tiles &t)
+{
+    r->tiles = t;
+    RveDesc &d = r->d;
+    d.zrows = t.zrows; d.yxt = t.yxt; d.xkc = t.xkc;
+    d.xkc3 = t.xkc3; d.zirows = t.zirows; d.zirows3 = t.zirows3;
+    r->plan_dirty = true;
+}
+
+int autotune_tiles(voce_rve *r)
+{
+    RveDesc &d = r->d;
+    const TileKey key{d.nx, d.ny, d.nz, d.mixed};
+    {
+        std::lock_guard<std::mutex> lock(g_tile_mu);
+        auto it = g_tile_cache.find(key);
+        if (it != g_tile_cache.end()) {
+            apply_tiles(r, it->second);
+            return VOCE_OK;
+        }
+    }
+    double *saved = nullptr;
+    CUDA_TRY(cudaMalloc(&saved, sizeof(double) * 6 * (size_t)d.nv));
+    CUDA_TRY(cudaMemcpyAsync(saved, d.dgs, sizeof(double) * 6 * (size_t)d.nv, cudaMemcpyDeviceToDevice, r->stream));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    Tiles best = r->tiles;
+    int rc = VOCE_OK;
+    const int phases[4] = {BP_ZF, BP_Y6, BP_XG, BP_ZI};
+    for (int ph : phases) {
+        int cand[8];
+        const int nc = tile_candidates(d, ph, cand, 8);
+        float best_ms = 1e30f;
+        int best_t = 0;
+        for (int c = 0; c < nc && rc == VOCE_OK; ++c) {
+            Tiles t = best;
+            switch (ph) {
+            case BP_ZF: t.zrows = cand[c]; break;
+            case BP_Y6: t.yxt = cand[c]; break;
+            case BP_XG: t.xkc = cand[c]; break;
+            default: t.zirows = cand[c]; break;
+            }
+            RveDesc dt = d;
+            dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc; dt.zirows = t.zirows;
+            std::vector<RveDesc> one(1, dt);
+            RveDesc *pd = nullptr;
+            int2 *pm = nullptr;
+            BatchPlan bp;
+            rc = make_plan(one, r->precision, pd, pm, bp);
+            if (rc) break;
+            float ms = 0.f;
+            cudaError_t e = launch_plan_phase(bp, ph, r->stream);    // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(e0, r->stream);
+            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch_plan_phase(bp, ph, r->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, r->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            cudaFree(pd);
+            cudaFree(pm);
+            if (e != cudaSuccess) {
+                rc = fail(VOCE_ERR_CUDA, "tile tuning: %s", cudaGetErrorString(e));
+                break;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_t = cand[c];
+            }
+        }
+        if (rc) break;
+        if (best_t > 0) {
+            switch (ph) {
+            case BP_ZF: best.zrows = best_t; break;
+            case BP_Y6: best.yxt = best_t; break;
+            case BP_XG: best.xkc = best_t; break;
+            default: best.zirows = best_t; break;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = cudaMemcpyAsync(d.dgs, saved, sizeof(double) * 6 * (size_t)d.nv, cudaMemcpyDeviceToDevice,
+                                    r->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+    cudaFree(saved);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "tile tuning: %s", cudaGetErrorString(e));
+    apply_tiles(r, best);
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    g_tile_cache[key] = best;
     return VOCE_OK;
 }
 
@@ -957,6 +1083,8 @@ int ensure_ring(voce_rve *r, int cap)
 }
 
 }  // namespace
+
+extern "C" {
 
 int voce_rve_run(voce_rve *r, int n)
 {
@@ -1381,6 +1509,44 @@ int voce_mesh_voronoi(const int dims[3], int n_seeds, const double *seeds_xyz,
         grain[v] = g + 1;
         phase[v] = 1;
     }
+    return VOCE_OK;
+}
+
+int voce_set_autotune(int on)
+{
+    g_autotune = on ? 1 : 0;
+    return VOCE_OK;
+}
+
+int voce_rve_get_tiles(const voce_rve *r, int tiles[6])
+{
+    if (!r || !tiles) return fail(VOCE_ERR_ARG, "null argument");
+    const Tiles &t = r->tiles;
+    tiles[0] = t.zrows; tiles[1] = t.yxt; tiles[2] = t.xkc;
+    tiles[3] = t.zirows; tiles[4] = t.xkc3; tiles[5] = t.zirows3;
+    return VOCE_OK;
+}
+
+int voce_rve_set_tiles(voce_rve *r, const int tiles[6])
+{
+    if (!r || !tiles) return fail(VOCE_ERR_ARG, "null argument");
+    if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch");
+    const RveDesc &d = r->d;
+    // each tile divides the dimension it splits, and its phase fits in shared memory
+    const int dim[6] = {d.ny, d.nx, d.ny, d.ny, d.ny, d.ny};
+    for (int k = 0; k < 6; ++k)
+        if (tiles[k] < 1 || dim[k] % tiles[k] != 0) return fail(VOCE_ERR_ARG, "tile %d = %d", k, tiles[k]);
+    Tiles t;
+    t.zrows = tiles[0]; t.yxt = tiles[1]; t.xkc = tiles[2];
+    t.zirows = tiles[3]; t.xkc3 = tiles[4]; t.zirows3 = tiles[5];
+    RveDesc dt = d;
+    dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc; dt.xkc3 = t.xkc3; dt.zirows = t.zirows; dt.zirows3 = t.zirows3;
+    for (int ph = BP_ZF; ph < BP_COUNT; ++ph)
+        if (batch_smem(dt, ph) > 227 * 1024) return fail(VOCE_ERR_ARG, "tiles need more shared memory than a block has");
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    apply_tiles(r, t);
+    if (r->graph_exec) { cudaGraphExecDestroy(r->graph_exec); r->graph_exec = nullptr; }
+    if (r->graph) { cudaGraphDestroy(r->graph); r->graph = nullptr; }
     return VOCE_OK;
 }
 

@@ -1662,6 +1662,61 @@ cudaError_t launch_plan_incr_end(const BatchPlan &bp, cudaStream_t s, Prof &pf)
     return cudaGetLastError();
 }
 
+template <typename R>
+static void plan_phase_t(const BatchPlan &bp, int phase, cudaStream_t s)
+{
+    const int FG = 152 * 4;
+    const RveDesc *D = bp.descs;
+    switch (phase) {
+    case BP_ZF:
+        kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
+        break;
+    case BP_Y6:
+        kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0);
+        break;
+    case BP_XG:
+        kb_fft_x_green<R><<<grid_for(bp.total[BP_XG], FG), 256, bp.smem[BP_XG], s>>>(D, bp.map[BP_XG], bp.total[BP_XG]);
+        break;
+    case BP_ZI:
+        kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
+        break;
+    default: break;
+    }
+}
+
+cudaError_t launch_plan_phase(const BatchPlan &bp, int phase, cudaStream_t s)
+{
+    if (bp.mixed) plan_phase_t<float>(bp, phase, s);
+    else plan_phase_t<double>(bp, phase, s);
+    return cudaGetLastError();
+}
+
+int tile_candidates(const RveDesc &d, int phase, int *out, int max)
+{
+    const bool f = d.mixed != 0;
+    const int B = f ? 4096 : 2048;
+    const size_t cs = f ? sizeof(float2) : sizeof(double2);
+    const size_t smem_max = 200 * 1024;
+    int n = 0;
+    for (int k = -2; k <= 2 && n < max; ++k) {
+        const int budget = k < 0 ? (B >> -k) : (B << k);
+        int t = 0;
+        size_t sm = 0;
+        switch (phase) {
+        case BP_ZF: t = pick_div<double>(d.ny, budget / (3 * d.nz)); sm = 2 * (size_t)d.nz * ((3 * t) | 1) * cs; break;
+        case BP_Y6: t = pick_div<double>(d.nx, budget / d.ny); sm = 2 * (size_t)d.ny * (t | 1) * cs; break;
+        case BP_XG: t = pick_div<double>(d.ny, (budget * 3 / 2) / (6 * d.nx)); sm = 2 * (size_t)d.nx * ((6 * t) | 1) * cs; break;
+        case BP_ZI: t = pick_div<double>(d.ny, budget / (3 * d.nz)); sm = 2 * (size_t)d.nz * ((3 * t) | 1) * cs; break;
+        default: return 0;
+        }
+        if (t < 1 || sm > smem_max) continue;
+        bool seen = false;
+        for (int i = 0; i < n; ++i) seen = seen || out[i] == t;
+        if (!seen) out[n++] = t;
+    }
+    return n;
+}
+
 cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond)
 {
     Prof none;

@@ -69,6 +69,12 @@ struct BatchPlan {
 void batch_units(const RveDesc &d, int units[BP_COUNT]);
 size_t batch_smem(const RveDesc &d, int phase);
 cudaError_t set_batch_smem(const BatchPlan &bp);
+// one forward-pass FFT phase (BP_ZF, BP_Y6 forward, BP_XG, BP_ZI) alone, for
+// tile tuning
+cudaError_t launch_plan_phase(const BatchPlan &bp, int phase, cudaStream_t s);
+// tile sizes worth trying for that phase of d (distinct, fitting in shared
+// memory); returns how many were written to out
+int tile_candidates(const RveDesc &d, int phase, int *out, int max);
 // one tick: prelude (pending), one Green iteration of every active RVE, the
 // increment end of every RVE that converged, the loop condition
 cudaError_t launch_batch_tick(const BatchPlan &bp, cudaStream_t s, cudaGraphConditionalHandle cond);
