@@ -119,6 +119,14 @@ class Group:
         return float(t.item())
 
 
+def whole_job_rate(grp, local_voxel_iterations: float, local_ms: float):
+    """Replicas: the voxel-iterations of all ranks over the slowest rank's
+    time.  Returns (voxel-iter/s, max ms, total voxel-iterations)."""
+    t_max = grp.max(local_ms)
+    vi = grp.sum(local_voxel_iterations)
+    return vi / (t_max * 1e-3), t_max, vi
+
+
 class Clocks:
     """nvidia-smi samples every 200 ms while the timed region runs."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -308,9 +316,7 @@ def run_voce(args, rank, world, grp):
     grp.barrier()
     launches = r.kernel_launches - launches0
     tot_ms = sum(step_ms)
-    t_max = grp.max(tot_ms)
-    vox_iters = grp.sum(float(nv * sum(iters)))
-    value = vox_iters / (t_max * 1e-3)
+    value, t_max, vox_iters = whole_job_rate(grp, float(nv * sum(iters)), tot_ms)
 
     # ---- per-kernel durations: CUDA events around every launch over the
     # next few increments (host-driven loop, same kernels, same stream) ----
