@@ -918,13 +918,18 @@ int autotune_tiles(voce_rve *r)
             BatchPlan bp;
             rc = make_plan(one, r->precision, pd, pm, bp);
             if (rc) break;
-            float ms = 0.f;
-            cudaError_t e = launch_plan_phase(bp, ph, r->stream);    // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(e0, r->stream);
-            for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = launch_plan_phase(bp, ph, r->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(e1, r->stream);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            // best of two rounds of 10 launches, after one warm-up launch
+            float ms = 1e30f;
+            cudaError_t e = launch_plan_phase(bp, ph, r->stream);
+            for (int round = 0; round < 2 && e == cudaSuccess; ++round) {
+                float t = 0.f;
+                e = cudaEventRecord(e0, r->stream);
+                for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = launch_plan_phase(bp, ph, r->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, r->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+                if (e == cudaSuccess && t < ms) ms = t;
+            }
             cudaFree(pd);
             cudaFree(pm);
             if (e != cudaSuccess) {

@@ -1362,12 +1362,11 @@ __global__ void __launch_bounds__(256) kb_fft_y(const RveDesc *descs, const int2
     }
 }
 
+// resident blocks per SM the Green pass is compiled for (registers): 3 with
+// the FP64 spectrum (measured faster despite some spilling), 2 with FP32
 template <typename R>
-// resident blocks per SM the Green pass is compiled for (registers)
-#ifndef VOCE_XG_BLOCKS
-#define VOCE_XG_BLOCKS 1
-#endif
-__global__ void __launch_bounds__(256, VOCE_XG_BLOCKS) kb_fft_x_green(const RveDesc *descs, const int2 *map, int total)
+__global__ void __launch_bounds__(256, sizeof(R) == 8 ? 3 : 2)
+kb_fft_x_green(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
