@@ -876,43 +876,62 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
     if (threadIdx.x != 0) return;
     MacroDev *m = d.macro;
     static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
+    // the macro inputs, loaded together; the updates are computed in
+    // registers and stored once (same operations, same order)
+    const int first_iter = m->first_iter, it = m->iter, istep = m->istep;
+    const double Err_e0 = m->Err_e, Err_s0 = m->Err_s, e_vm = m->e_vm;
+    double dg[9], acum[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        dg[q] = m->dDisGradAvg[q];   // entries get_smacro leaves alone keep their value
+        acum[q] = m->dDisGradAvg_acum[q];
+    }
     // the mixed form's Newton ran in single precision alone this iteration
     // (the predicate nr_unit used): it may not end the increment
-    const bool fp32_only =
-        d.nr32 && (m->first_iter || fmax(fabs(m->Err_e), fabs(m->Err_s)) > VOCE_POLISH_ERR);
+    const bool fp32_only = d.nr32 && (first_iter || fmax(fabs(Err_e0), fabs(Err_s0)) > VOCE_POLISH_ERR);
     double Err_e = tot[1] * d.wgt, Err_s = tot[0] * d.wgt;
-    double s9[9], s19[9];
+    double s9[9], s19[9], sa[9], sa1[9];
     sym9_from_b(tot + 2, s9);
     sym9_from_b(tot + 8, s19);
+#pragma unroll
     for (int q = 0; q < 9; ++q) {
-        m->SigAvg[q] = s9[q] * d.wgt;
-        m->SigAvg1[q] = s19[q] * (d.wgt / d.wgt_ph1);
+        sa[q] = s9[q] * d.wgt;
+        sa1[q] = s19[q] * (d.wgt / d.wgt_ph1);
+        m->SigAvg[q] = sa[q];
+        m->SigAvg1[q] = sa1[q];
     }
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
         const int ii = IJV[0][i], jj = IJV[1][i];
         double s = 0.0;
         if (d.vflag[i] == 0)
+#pragma unroll
             for (int k = 0; k < 6; ++k) {
                 const int kk = IJV[0][k], ll = IJV[1][k];
                 s += d.S0t[((ii * 3 + jj) * 3 + kk) * 3 + ll] * d.sflag[k] *
-                     (d.Scauchy[kk * 3 + ll] - m->SigAvg[kk * 3 + ll]);
+                     (d.Scauchy[kk * 3 + ll] - sa[kk * 3 + ll]);
             }
-        m->dDisGradAvg[ii * 3 + jj] = s;
+        dg[ii * 3 + jj] = s;
     }
-    for (int q = 0; q < 9; ++q) m->dDisGradAvg_acum[q] += m->dDisGradAvg[q];
-    m->s_vm = svm_of(m->SigAvg);
-    m->s_vm1 = svm_of(m->SigAvg1);
-    if (fabs(m->e_vm) > 1E-5) Err_e /= m->e_vm;
-    Err_s /= m->s_vm;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        acum[q] += dg[q];
+        m->dDisGradAvg[q] = dg[q];
+        m->dDisGradAvg_acum[q] = acum[q];
+    }
+    const double svm = svm_of(sa), svm1 = svm_of(sa1);
+    m->s_vm = svm;
+    m->s_vm1 = svm1;
+    if (fabs(e_vm) > 1E-5) Err_e /= e_vm;
+    Err_s /= svm;
     m->Err_e = Err_e;
     m->Err_s = Err_s;
-    const int it = m->iter;
     if (it < d.iter_max) {
-        const int slot = (m->istep - 1) % d.incr_cap;
+        const int slot = (istep - 1) % d.incr_cap;
         double *lg = d.itlog + ((long long)slot * d.iter_max + it) * VOCE_ITLOG;
         lg[0] = Err_e;
         lg[1] = Err_s;
-        lg[2] = m->s_vm;
+        lg[2] = svm;
         lg[3] = tot[14];
         lg[4] = tot[1];   // raw sum of the strain-compatibility norms
         lg[5] = tot[0];   // raw sum of the stress-change norms
@@ -922,19 +941,18 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
     m->iter_total += 1;
     m->nr_total += tot[14];
     m->nr_max = max(m->nr_max, (int)tot[15]);
-    const double *g = m->dDisGradAvg;
-    double t6[6] = {g[0], g[4], g[8], 0.5 * (g[5] + g[7]), 0.5 * (g[2] + g[6]), 0.5 * (g[1] + g[3])};
+    double t6[6] = {dg[0], dg[4], dg[8], 0.5 * (dg[5] + dg[7]), 0.5 * (dg[2] + dg[6]), 0.5 * (dg[1] + dg[3])};
     t6_to_b<double>(t6, m->ddg6);
     m->first_iter = 0;
     m->pending_prelude = 0;
-    const bool more = (m->iter < d.iter_max) &&
+    const bool more = (it + 1 < d.iter_max) &&
                       (fp32_only || fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
     m->converged = more ? 0 : 1;
     if (!more) {
         // epilogue macro bookkeeping (evolution.c:438-461)
         double act[9], vga[9];
         for (int q = 0; q < 9; ++q) {
-            act[q] = m->DisGradAvg[q] + m->dDisGradAvg_acum[q];
+            act[q] = m->DisGradAvg[q] + acum[q];
             vga[q] = (act[q] - m->DisGradAvg_t[q]) / d.dt;
         }
         for (int q = 0; q < 9; ++q) {
@@ -953,7 +971,7 @@ __device__ void finalize_iter_body(const RveDesc &d, int npart)
         // increment except the last one, which get_smacro computes after the
         // final update (evolution.c:391 vs :418): only those enter VelGrad
         double a[9];
-        for (int q = 0; q < 9; ++q) a[q] = m->dDisGradAvg_acum[q] - m->dDisGradAvg[q];
+        for (int q = 0; q < 9; ++q) a[q] = acum[q] - dg[q];
         m->acum_a[0] = 0.5 * (a[5] - a[7]);
         m->acum_a[1] = 0.5 * (a[2] - a[6]);
         m->acum_a[2] = 0.5 * (a[1] - a[3]);
