@@ -67,6 +67,7 @@ def parse():
                    help="default: fp64 (cfg2), mixed_nr32 (cfg3, cfg4, cfg5)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--rves", type=int, default=512, help="cfg4: RVEs in the batch")
+    p.add_argument("--edge", type=int, default=256, help="cfg3: grid edge (radix 2/3 only)")
     p.add_argument("--increments", type=int, default=2,
                    help="cfg4: whole increments every RVE runs in the timed batch")
     p.add_argument("--requests", type=int, default=32, help="cfg5: requests in the sample")
@@ -430,7 +431,7 @@ def run_cfg3(args):
     chosen = args.precision or "mixed_nr32"
     t0 = time.perf_counter()
     # config 3 (synth.config3), its mesh tessellated on the GPU
-    case = synth.Case("cfg3_256", _voronoi_mesh(256, 4096, 3), synth.CU_LIKE,
+    case = synth.Case("cfg3_%d" % args.edge, _voronoi_mesh(args.edge, 4096, 3), synth.CU_LIKE,
                       synth.plane_strain_compression(), 0.2, 250)
     t_mesh = time.perf_counter() - t0
     d = tempfile.mkdtemp(prefix="cfg3_")
@@ -479,7 +480,7 @@ def run_cfg3(args):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": a["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPE[chosen], "data": "synthetic",
-        "config": {"workload": "256^3 periodic Voronoi, 4096 grains, Cu FCC, plane-strain "
+        "config": {"workload": "%d^3 periodic Voronoi, 4096 grains, Cu FCC, plane-strain " % args.edge +
                                "compression Lzz=-1e-3/s Lxx=+1e-3/s, 2e-4 per increment "
                                "(config 3), %s form" % chosen, "voxels": nv,
                    "mesh_generation_s": t_mesh, "l2": "flushed before every step"},

@@ -32,6 +32,12 @@
 // this (and the first of every increment) run the Newton solve in single
 // precision only; the rest end it on the double-precision residual.
 #define VOCE_POLISH_ERR 1e-4
+// systems per unrolled step of the single-precision flow-rule loops (their
+// loads issue together)
+#ifndef VOCE_SYS_UNROLL
+#define VOCE_SYS_UNROLL 2
+#endif
+constexpr int kSysUnroll = VOCE_SYS_UNROLL;
 
 // Lebensohn-Tome basis constants, the literal values of kinematics.c:333-335
 #define RSQ2 0.70710678118654744
@@ -317,6 +323,7 @@ __device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, long long v, con
     for (int i = 0; i < 5; ++i) edot[i] = 0.0f;
 #pragma unroll
     for (int i = 0; i < 15; ++i) D[i] = 0.0f;
+#pragma unroll kSysUnroll
     for (int k = 0; k < d.nsys; ++k) {
         float sc[5];
 #pragma unroll

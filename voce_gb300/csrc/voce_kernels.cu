@@ -589,6 +589,7 @@ __device__ __forceinline__ void edot_fp64(const RveDesc &d, long long v, const d
 #pragma unroll
     for (int i = 0; i < 5; ++i) edot[i] = 0.0;
     const bool n20 = d.ipow_n == 20, uni = d.gam0_uniform != 0;
+#pragma unroll kSysUnroll
     for (int k = 0; k < d.nsys; ++k) {
         double sc[5];
 #pragma unroll
