@@ -60,6 +60,9 @@ double voce_measure_fp64_tflops(void);
  * voce_rve_get_tiles: the z-forward, y, x/Green, z-inverse tiles and the two
  * antisymmetric back-transform tiles of r. */
 int voce_set_autotune(int on);
+/* With VOCE_TILE_CACHE=<file> in the environment the choices are read from
+ * that file first and new ones appended to it (one line per shape), so that
+ * other processes on the machine use the same tiles. */
 int voce_rve_get_tiles(const voce_rve *r, int tiles[6]);
 /* Force the tiles (each divides the dimension it splits: ny, nx, ny, ny, ny,
  * ny; all phases fit in shared memory); between calls, outside a batch. */

@@ -48,3 +48,28 @@ def test_tuning_can_be_switched_off(voce_lib):
     with capi.Rve.from_files(nl) as r:
         with pytest.raises(capi.VoceError):
             r.set_tiles([3, 1, 1, 1, 1, 1])      # 3 does not divide 8
+
+
+def test_tile_cache_file_is_shared_between_processes(voce_lib):
+    """VOCE_TILE_CACHE: the first process records its tuned tiles, a second
+    one (with tuning timings that could differ, e.g. under a profiler) reads
+    and uses them."""
+    import os
+    import subprocess
+    import sys
+    case = synth.small_case(12, 6, 83, n_steps=1)
+    nl = case.write(tempfile.mkdtemp(prefix="tiles_"))
+    cache = os.path.join(tempfile.mkdtemp(prefix="tilecache_"), "tiles.txt")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    prog = ("import sys; sys.path.insert(0, %r)\n"
+            "from voce_gb300 import capi\n"
+            "r = capi.Rve.from_files(%r)\n"
+            "print(','.join(map(str, r.tiles())))\n" % (root, nl))
+    env = dict(os.environ, VOCE_TILE_CACHE=cache)
+    a = subprocess.run([sys.executable, "-c", prog], env=env, capture_output=True, text=True, check=True)
+    lines = open(cache).read().split("\n")
+    assert lines[0].startswith("12 12 12 0 ")
+    # the second process finds the shape in the file: no new line, same tiles
+    b = subprocess.run([sys.executable, "-c", prog], env=env, capture_output=True, text=True, check=True)
+    assert a.stdout == b.stdout
+    assert open(cache).read().count("\n") == 1

@@ -876,12 +876,45 @@ void apply_tiles(voce_rve *r, const Tiles &t)
     r->plan_dirty = true;
 }
 
+// VOCE_TILE_CACHE=<file>: tile choices are read from the file before any
+// tuning and each new choice is appended, so that another process on the
+// same machine (a profiler's run of the same command, say) uses the same
+// tiles.  One line per shape: nx ny nz mixed zrows yxt xkc xkc3 zirows zirows3.
+bool g_tile_file_read = false;
+
+void read_tile_file()
+{
+    g_tile_file_read = true;
+    const char *path = std::getenv("VOCE_TILE_CACHE");
+    if (!path || !path[0]) return;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return;
+    TileKey k;
+    Tiles t;
+    while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d", &k.nx, &k.ny, &k.nz, &k.mixed, &t.zrows, &t.yxt,
+                       &t.xkc, &t.xkc3, &t.zirows, &t.zirows3) == 10)
+        g_tile_cache[k] = t;
+    std::fclose(f);
+}
+
+void append_tile_file(const TileKey &k, const Tiles &t)
+{
+    const char *path = std::getenv("VOCE_TILE_CACHE");
+    if (!path || !path[0]) return;
+    FILE *f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d\n", k.nx, k.ny, k.nz, k.mixed, t.zrows, t.yxt, t.xkc, t.xkc3,
+                 t.zirows, t.zirows3);
+    std::fclose(f);
+}
+
 int autotune_tiles(voce_rve *r)
 {
     RveDesc &d = r->d;
     const TileKey key{d.nx, d.ny, d.nz, d.mixed};
     {
         std::lock_guard<std::mutex> lock(g_tile_mu);
+        if (!g_tile_file_read) read_tile_file();
         auto it = g_tile_cache.find(key);
         if (it != g_tile_cache.end()) {
             apply_tiles(r, it->second);
@@ -962,6 +995,7 @@ int autotune_tiles(voce_rve *r)
     apply_tiles(r, best);
     std::lock_guard<std::mutex> lock(g_tile_mu);
     g_tile_cache[key] = best;
+    append_tile_file(key, best);
     return VOCE_OK;
 }
 
