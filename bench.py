@@ -72,6 +72,9 @@ def parse():
                    help="cfg4: whole increments every RVE runs in the timed batch")
     p.add_argument("--requests", type=int, default=32, help="cfg5: requests in the sample")
     p.add_argument("--rate", type=float, default=2.0, help="cfg5: Poisson arrival rate, req/s")
+    p.add_argument("--budget-gb", type=float, default=200.0, help="cfg5: server HBM budget, GB")
+    p.add_argument("--quantum", type=int, default=0,
+                   help="cfg5: ticks after which a running request may be suspended (0: never)")
     p.add_argument("--inc-scale", type=float, default=0.1,
                    help="cfg5: increments per request = round(scale x U{10..80})")
     p.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
@@ -677,8 +680,11 @@ def run_cfg5(args):
         nl, sx = _rve_inputs(c, d, str(i))
         reqs.append((t_arr, c, nl, sx, inc))
 
+    preempt = [0]
+
     def serve(precision, one_at_a_time):
-        budget = 200 << 30
+        preempt[0] = 0
+        budget = int(args.budget_gb * (1 << 30))
         lat, vi = [], 0
         t0 = time.perf_counter()
         if one_at_a_time:
@@ -696,6 +702,7 @@ def run_cfg5(args):
             span = time.perf_counter() - t0
             return lat, vi, span
         with capi.Server(precision, budget, ticks_per_round=16) as s:
+            s.set_quantum(args.quantum)
             ids = []
             k = 0
             while True:
@@ -718,6 +725,7 @@ def run_cfg5(args):
                 # arrival -> done: time in the server plus the poll delay before submission
                 lat.append((info.t_done - info.t_submit) + (sub_wall - ta))
                 vi += info.voxel_iterations
+                preempt[0] += info.preemptions
         return lat, vi, span
 
     chosen = args.precision or "mixed_nr32"
@@ -728,6 +736,8 @@ def run_cfg5(args):
         lat, vi, span = serve(prec, single)
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "throughput": vi / span, "makespan_s": span, "voxel_iterations": vi}
+        if not single:
+            out[name]["preemptions"] = preempt[0]
     b = out["plain_fp64_one_at_a_time"]
     for name, a in out.items():
         if name != "plain_fp64_one_at_a_time":
@@ -742,7 +752,8 @@ def run_cfg5(args):
         "config": {"workload": "serving: %d Poisson requests at %.2f req/s, edges U{16,32,64,128}, "
                                "grains log-U[8,2048], random traceless loads, increments "
                                "round(%.2f x U{10..80}) (config 5 sample), continuous batching, "
-                               "%s form" % (len(reqs), args.rate, args.inc_scale, chosen)},
+                               "%s form" % (len(reqs), args.rate, args.inc_scale, chosen),
+                   "hbm_budget_gb": args.budget_gb, "quantum_ticks": args.quantum},
         "served": out,
         "throughput_ratio": a["throughput_ratio"], "p50_ratio": a["p50_ratio"],
         "p99_ratio": a["p99_ratio"],

@@ -29,8 +29,10 @@ int voce_batch_create(int precision, voce_batch **out);
  * voce_rve_create*) inside the batch.  While it belongs to a batch an RVE is
  * advanced only by voce_batch_run. */
 int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments);
-/* Take r out (allowed between increments); it keeps its state and can run
- * alone again. */
+/* Take r out after any voce_batch_run; it keeps its state and can run alone
+ * again, be snapshotted or join another batch.  Taken out in the middle of
+ * an increment it continues that increment where it stopped (voce_rve_run(n)
+ * and voce_batch_add(.., n) count it as the first of their n). */
 int voce_batch_remove(voce_batch *b, voce_rve *r);
 int voce_batch_size(const voce_batch *b);
 /* Run up to max_ticks ticks; *active_left receives the number of RVEs that

@@ -35,6 +35,7 @@ typedef struct {
     double t_submit, t_admit, t_done;
     long long voxel_iterations; /* sum over its increments of voxels x Green iterations */
     voce_increment last;        /* record of its last increment */
+    int preemptions;            /* times it was suspended to make room */
 } voce_request_info;
 
 /* keep_fields: keep the final stress and strain-rate fields (Voigt order,
@@ -45,6 +46,14 @@ int voce_server_create(int precision, long long hbm_budget_bytes,
 int voce_server_submit(voce_server *s, const voce_namelist *nl,
                        const voce_slip *slip[2], const voce_mesh *mesh,
                        int n_increments, long long *id_out);
+/* Time slicing under a full budget: when the request at the head of the
+ * queue does not fit, a running request that has run at least `ticks` batch
+ * ticks since its admission (the longest-running first) is suspended -- its
+ * state goes to host memory as a snapshot, it frees its device memory and
+ * rejoins the back of the queue -- until the head fits.  A suspended request
+ * resumes exactly where it stopped (bit-identical results).  0 (the
+ * default): no suspension, first in first out. */
+int voce_server_set_quantum(voce_server *s, int ticks);
 /* One round; *running and *queued receive the counts afterwards. */
 int voce_server_poll(voce_server *s, int *running, int *queued);
 double voce_server_now(const voce_server *s);

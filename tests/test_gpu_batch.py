@@ -113,3 +113,34 @@ def test_profiled_ticks_equal_graph_ticks(voce_lib):
             assert all(n == 0 for _, n in kt.values())
     for a, b_ in zip(*snaps):
         _same(a, b_)
+
+
+def test_removed_mid_increment_continues_alone_or_elsewhere(voce_lib):
+    """Taken out of a batch in the middle of an increment, an RVE finishes
+    that increment where it stopped: alone, or (through a snapshot) in
+    another batch -- the same results as never having left."""
+    cases = _cases()[:2]
+    ref = []
+    for c, n in cases:
+        with _make(c, capi.PREC_FP64) as r:
+            r.run(2)
+            ref.append(_snapshot(r, 2))
+    rves = [_make(c, capi.PREC_FP64) for c, _ in cases]
+    with capi.Batch(capi.PREC_FP64) as b:
+        for r in rves:
+            b.add(r, 2)
+        b.run(max_ticks=7)                   # both are mid-increment now
+        for r in rves:
+            assert r.increments_done == 0
+            b.remove(r)
+    rves[0].run(2)                           # the partial increment + one more
+    _same(_snapshot(rves[0], 2), ref[0])
+    blob = rves[1].snapshot()
+    rves[1].close()
+    r1 = capi.Rve.restore(blob)
+    with capi.Batch(capi.PREC_FP64) as b2:
+        b2.add(r1, 2)
+        assert b2.run() == 0
+    _same(_snapshot(r1, 2), ref[1])
+    rves[0].close()
+    r1.close()

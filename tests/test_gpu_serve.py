@@ -62,3 +62,41 @@ def test_request_larger_than_budget_fails(voce_lib):
         s.poll()
         info = s.info(rid)
         assert info.status == capi.REQ_FAILED and info.error == 7
+
+
+def test_time_slicing_suspends_and_resumes_bit_for_bit(voce_lib):
+    """A budget for two requests, three requests and a quantum of 3 ticks:
+    running requests are suspended to host memory to let the queue move, and
+    every result still equals the request solved alone."""
+    rng = np.random.Generator(np.random.PCG64(78))
+    cases = []
+    for i in range(3):
+        c = synth.small_case(16, 8, 600 + i, n_steps=2, load=synth.random_traceless_load(rng))
+        c.iter_max = 30
+        cases.append((c, 2))
+    alone = []
+    for c, n in cases:
+        nlp, _, _ = _inputs(c)
+        with capi.Rve.from_files(nlp) as r:
+            r.run(n)
+            alone.append(([r.increment(k) for k in range(n)], r.field("sig_voigt")))
+    budget = 2 * capi.footprint((16, 16, 16))
+    with capi.Server(capi.PREC_FP64, budget, ticks_per_round=2, keep_fields=True) as s:
+        s.set_quantum(3)
+        ids = []
+        for c, n in cases:
+            _, nl, sx = _inputs(c)
+            ids.append(s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, n))
+        for _ in range(100000):
+            run, que = s.poll()
+            assert s.bytes_in_use <= budget
+            if run == 0 and que == 0:
+                break
+        pre = 0
+        for rid, (c, n), (incs, sig) in zip(ids, cases, alone):
+            info = s.info(rid)
+            assert info.status == capi.REQ_DONE and info.increments_done == n
+            assert info.last.iters == incs[-1]["iters"] and list(info.last.sig_avg) == incs[-1]["sig_avg"]
+            assert np.array_equal(s.result(rid, "sig_voigt", c.mesh.nvox), sig)
+            pre += info.preemptions
+        assert pre > 0

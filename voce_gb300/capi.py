@@ -158,6 +158,7 @@ PROTOTYPES = [
     ("voce_set_autotune", C.c_int, [C.c_int]),
     ("voce_rve_get_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("voce_server_set_quantum", C.c_int, [C.c_void_p, C.c_int]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -519,7 +520,7 @@ class RequestInfo(C.Structure):
                 ("increments_done", C.c_int), ("increments_wanted", C.c_int),
                 ("dims", C.c_int * 3), ("t_submit", C.c_double), ("t_admit", C.c_double),
                 ("t_done", C.c_double), ("voxel_iterations", C.c_longlong),
-                ("last", VoceIncrement)]
+                ("last", VoceIncrement), ("preemptions", C.c_int)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -551,6 +552,9 @@ class Server:
         _check(load().voce_server_submit(self._h, C.byref(nl), sp, C.byref(mesh), n_increments,
                                          C.byref(rid)))
         return rid.value
+
+    def set_quantum(self, ticks: int) -> None:
+        _check(load().voce_server_set_quantum(self._h, ticks))
 
     def poll(self):
         run = C.c_int()

@@ -1812,8 +1812,13 @@ int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments)
     if (r->precision != b->precision) return fail(VOCE_ERR_ARG, "precision differs from the batch's");
     int rc = ensure_ring(r, n_increments + 1);
     if (rc) return rc;
-    // the RVE is at an increment boundary: its next prelude is pending
-    rc = set_macro_flags(r, 1, r->n_done + n_increments, 1);
+    // at an increment boundary the next prelude is pending; an RVE taken out
+    // of a batch in the middle of an increment continues that increment
+    // (it counts as the first of the n)
+    MacroDev m;
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    CUDA_TRY(cudaMemcpy(&m, r->d.macro, sizeof(m), cudaMemcpyDeviceToHost));
+    rc = set_macro_flags(r, 1, r->n_done + n_increments, m.iter != 0 ? 0 : 1);
     if (rc) return rc;
     r->batch = b;
     b->rves.push_back(r);
@@ -1827,11 +1832,11 @@ int voce_batch_remove(voce_batch *b, voce_rve *r)
     MacroDev m;
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(cudaMemcpy(&m, r->d.macro, sizeof(m), cudaMemcpyDeviceToHost));
-    if (m.active && m.iter != 0) return fail(VOCE_ERR_STATE, "the RVE is in the middle of an increment");
     int rc = collect_new(r, false);
     if (rc) return rc;
-    // between increments the next increment's prelude has not run yet
-    rc = set_macro_flags(r, 1, 0x7fffffff, 1);
+    // between increments the next increment's prelude has not run yet; in
+    // the middle of one it has, and the increment goes on where it stopped
+    rc = set_macro_flags(r, 1, 0x7fffffff, m.iter != 0 ? 0 : 1);
     if (rc) return rc;
     b->rves.erase(std::find(b->rves.begin(), b->rves.end(), r));
     r->batch = nullptr;
@@ -1918,7 +1923,10 @@ int voce_batch_destroy(voce_batch *b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (voce_rve *r : b->rves) {
         collect_new(r, false);
-        set_macro_flags(r, 1, 0x7fffffff, 1);
+        MacroDev m;
+        const bool mid = cudaMemcpy(&m, r->d.macro, sizeof(m), cudaMemcpyDeviceToHost) == cudaSuccess &&
+                         m.iter != 0;
+        set_macro_flags(r, 1, 0x7fffffff, mid ? 0 : 1);
         r->batch = nullptr;
     }
     delete b;

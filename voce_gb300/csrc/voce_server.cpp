@@ -3,6 +3,7 @@
 #include "voce_gpu.h"
 #include "voce_serve.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -23,6 +24,8 @@ struct Request {
     voce_rve *rve = nullptr;
     long long footprint = 0;
     std::vector<double> sig, edot;  // kept fields (Voigt, 6 x nvox)
+    std::vector<char> snap;         // state while suspended (voce_rve_snapshot)
+    long long ticks_run = 0;        // batch ticks since its last admission
 };
 
 }  // namespace
@@ -31,6 +34,7 @@ struct voce_server {
     int precision = 0;
     long long budget = 0, in_use = 0;
     int ticks_per_round = 1;
+    int quantum = 0;                // ticks before a running request may be suspended
     bool keep_fields = false;
     voce_batch *batch = nullptr;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
@@ -45,6 +49,30 @@ struct voce_server {
 };
 
 namespace {
+
+// Move a running request's state to host memory (a snapshot) and free its
+// device memory; it goes to the back of the queue and resumes, bit for bit,
+// when admitted again.
+int suspend(voce_server *s, Request &q)
+{
+    int rc = voce_batch_remove(s->batch, q.rve);
+    if (rc) return rc;
+    const long long n = voce_rve_snapshot_size(q.rve);
+    if (n < 0) return (int)-n;
+    q.snap.resize((size_t)n);
+    rc = voce_rve_snapshot(q.rve, q.snap.data(), n);
+    if (rc) return rc;
+    q.info.increments_done = voce_rve_increments_done(q.rve);
+    voce_rve_destroy(q.rve);
+    q.rve = nullptr;
+    s->in_use -= q.footprint;
+    q.info.status = VOCE_REQ_QUEUED;
+    q.info.preemptions += 1;
+    q.ticks_run = 0;
+    s->running.erase(std::find(s->running.begin(), s->running.end(), q.info.id));
+    s->queue.push_back(q.info.id);
+    return VOCE_OK;
+}
 
 void retire(voce_server *s, Request &q, int error)
 {
@@ -135,7 +163,8 @@ int voce_server_submit(voce_server *s, const voce_namelist *nl, const voce_slip 
 int voce_server_poll(voce_server *s, int *running, int *queued)
 {
     if (!s) return VOCE_ERR_ARG;
-    // admission: first in, first out, while the footprint fits
+    // admission: first in, first out, while the footprint fits; with a
+    // quantum, requests that have run that long make room by suspending
     while (!s->queue.empty()) {
         Request &q = *s->reqs[s->queue.front()];
         if (q.footprint > s->budget) {
@@ -143,16 +172,37 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
             retire(s, q, VOCE_ERR_NOMEM);
             continue;
         }
-        if (s->in_use + q.footprint > s->budget) break;
+        if (s->in_use + q.footprint > s->budget) {
+            Request *victim = nullptr;
+            if (s->quantum > 0)
+                for (long long id : s->running) {
+                    Request &c = *s->reqs[id];
+                    if (c.ticks_run >= s->quantum && (!victim || c.ticks_run > victim->ticks_run)) victim = &c;
+                }
+            if (!victim) break;
+            int rc = suspend(s, *victim);
+            if (rc) return rc;
+            continue;
+        }
         s->queue.pop_front();
-        voce_mesh m;
-        std::memcpy(m.dims, q.info.dims, sizeof(m.dims));
-        m.euler_deg = q.euler.data();
-        m.grain = q.grain.data();
-        m.phase = q.phase.data();
-        const voce_slip *sp[2] = {q.has_slip[0] ? &q.slip[0] : nullptr, q.has_slip[1] ? &q.slip[1] : nullptr};
-        int rc = voce_rve_create(&q.nl, sp, &m, s->precision, &q.rve);
-        if (rc == VOCE_OK) rc = voce_batch_add(s->batch, q.rve, q.info.increments_wanted);
+        int rc = VOCE_OK;
+        if (!q.snap.empty()) {
+            // a suspended request: its state comes back from the snapshot
+            rc = voce_rve_restore(q.snap.data(), (long long)q.snap.size(), &q.rve);
+            if (rc == VOCE_OK) std::vector<char>().swap(q.snap);
+        } else {
+            voce_mesh m;
+            std::memcpy(m.dims, q.info.dims, sizeof(m.dims));
+            m.euler_deg = q.euler.data();
+            m.grain = q.grain.data();
+            m.phase = q.phase.data();
+            const voce_slip *sp[2] = {q.has_slip[0] ? &q.slip[0] : nullptr,
+                                      q.has_slip[1] ? &q.slip[1] : nullptr};
+            rc = voce_rve_create(&q.nl, sp, &m, s->precision, &q.rve);
+        }
+        // increments still to do (one in progress counts as the first)
+        if (rc == VOCE_OK)
+            rc = voce_batch_add(s->batch, q.rve, q.info.increments_wanted - voce_rve_increments_done(q.rve));
         if (rc != VOCE_OK) {
             if (q.rve) { voce_rve_destroy(q.rve); q.rve = nullptr; }
             retire(s, q, rc);
@@ -160,13 +210,17 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
         }
         s->in_use += q.footprint;
         q.info.status = VOCE_REQ_RUNNING;
-        q.info.t_admit = s->now();
+        if (q.info.preemptions == 0) q.info.t_admit = s->now();
+        q.ticks_run = 0;
         s->running.push_back(q.info.id);
     }
     if (!s->running.empty()) {
         int left = 0;
+        const long long t0 = voce_batch_ticks(s->batch);
         int rc = voce_batch_run(s->batch, s->ticks_per_round, &left);
         if (rc) return rc;
+        const long long ran = voce_batch_ticks(s->batch) - t0;
+        for (long long id : s->running) s->reqs[id]->ticks_run += ran;
         std::vector<long long> still;
         for (long long id : s->running) {
             Request &q = *s->reqs[id];
@@ -183,6 +237,13 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
 }
 
 double voce_server_now(const voce_server *s) { return s ? s->now() : -1.0; }
+
+int voce_server_set_quantum(voce_server *s, int ticks)
+{
+    if (!s || ticks < 0) return VOCE_ERR_ARG;
+    s->quantum = ticks;
+    return VOCE_OK;
+}
 
 int voce_server_info(const voce_server *s, long long id, voce_request_info *out)
 {
