@@ -401,7 +401,11 @@ int alloc_device(voce_rve *r)
     d.sch32 = nullptr;
     d.itau32 = nullptr;
     d.sgp32 = nullptr;
-    if (d.nr32) { AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv); }
+    d.sch_lo = d.itau_lo = d.sgp_lo = nullptr;
+    if (d.nr32) {
+        AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv);
+        AL(d.sch_lo, 60 * nv); AL(d.itau_lo, 24 * nv); AL(d.sgp_lo, 21 * nv);
+    }
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
     AL(d.macro, 1);
     d.incr_cap = 32;   // increments per host read-back
@@ -451,6 +455,9 @@ void for_state(RveDesc &d, F &&f)
         f((void **)&d.sch32, 60 * nv * S);
         f((void **)&d.itau32, 24 * nv * S);
         f((void **)&d.sgp32, 21 * nv * S);
+        f((void **)&d.sch_lo, 60 * nv * S);
+        f((void **)&d.itau_lo, 24 * nv * S);
+        f((void **)&d.sgp_lo, 21 * nv * S);
     }
     // the antisymmetric Green update summed over the current increment's
     // iterations, and the macro state
@@ -471,7 +478,8 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
     // + the FP64 form's stored Green-operator frequencies, 9 doubles each
-    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 420 : 0)) + nspec * 9 * cplx +
+    // + the mixed_nr32 form's float pairs of sch, itau and S_g + S0 (2 x 105 floats)
+    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 840 : 0)) + nspec * 9 * cplx +
            (precision == VOCE_PREC_FP64 ? nspec * 9 * 8 : 0);
 }
 
@@ -538,6 +546,8 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     d.iter_max = nl->IterMax;
     d.err_tol = nl->Err;
     d.dt = nl->TimeStep;
+    d.dth = (float)d.dt;
+    d.dtl = (float)(d.dt - (double)d.dth);
     const int Nxyz = nx * ny * nz;
     d.wgt = 1. / Nxyz;
     d.inv_nv = 1.0 / (double)Nxyz;
@@ -571,6 +581,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         d.g0n[s] = sx.gamd0 * nr;
         d.gam0f[s] = (float)sx.gamd0;
         d.nrsf[s] = (float)nr;
+        d.gam0l[s] = (float)(sx.gamd0 - (double)d.gam0f[s]);
         d.gam0_uniform = 1;   // one slip mode per phase: one gam0
         d.tau0[s] = sx.tau0f;
         d.tau0b[s] = sx.tau0b;
@@ -1330,7 +1341,7 @@ long long snapshot_write(voce_rve *r, char *out)
     SnapHead h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, kSnapMagic, 8);
-    h.version = 1;
+    h.version = 2;
     h.desc_size = sizeof(RveDesc);
     h.macro_size = sizeof(MacroDev);
     h.nl_size = sizeof(voce_namelist);
@@ -1402,7 +1413,7 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
     if (size < (long long)sizeof(h)) return fail(VOCE_ERR_PARSE, "snapshot too short");
     std::memcpy(&h, in, sizeof(h));
     if (std::memcmp(h.magic, kSnapMagic, 8) != 0) return fail(VOCE_ERR_PARSE, "not an RVE snapshot");
-    if (h.version != 1 || h.desc_size != sizeof(RveDesc) || h.macro_size != sizeof(MacroDev) ||
+    if (h.version != 2 || h.desc_size != sizeof(RveDesc) || h.macro_size != sizeof(MacroDev) ||
         h.nl_size != sizeof(voce_namelist) || h.incr_size != sizeof(voce_increment))
         return fail(VOCE_ERR_UNSUPPORTED, "snapshot written by a different build of the library");
     if (h.total != size) return fail(VOCE_ERR_PARSE, "snapshot of %lld bytes, header says %lld", size, (long long)h.total);

@@ -89,6 +89,8 @@ struct RveDesc {
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
     float gam0f[VOCE_NS], nrsf[VOCE_NS];   // float copies for the mixed Newton
+    float gam0l[VOCE_NS];                  // gam0 - gam0f, rounded to float
+    float dth, dtl;                        // dt as a float pair: dth + dtl
     int gam0_uniform;    // every system has the same gam0
     double tau0[VOCE_NS], tau1[VOCE_NS], thet0[VOCE_NS], thet1[VOCE_NS];
     double hard[VOCE_NS * VOCE_NS];
@@ -114,6 +116,7 @@ struct RveDesc {
     float *sch32;        // float copy of sch (mixed-precision Newton only)
     float *itau32;       // float copy of itau (mixed-precision Newton only)
     float *sgp32;        // float (S_g + S0), packed upper triangle (mixed-precision Newton only)
+    float *sch_lo, *itau_lo, *sgp_lo;   // x - (double)x32 rounded to float, for the same three
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;
@@ -311,14 +314,21 @@ __device__ __forceinline__ float pow_abs_ef(float a, int e)
     return res;
 }
 
+// The single-precision Newton kernel stages each voxel's float Schmid
+// vectors and 1/CRSS (both directions) in shared memory, one column per
+// thread: st[c * VOCE_NR_THREADS], c = 5k+i for the Schmid vectors and
+// VOCE_STAGE_ITAU + 2k + (rss < 0) for 1/CRSS.
+#define VOCE_NR_THREADS 128
+#define VOCE_STAGE_ITAU 60
+#define VOCE_STAGE_FLOATS 84
+
 // flow_rule entirely in single precision (mixed-precision Newton, integer
 // exponent only): strain rate and its 5x5 Jacobian (packed upper triangle)
-// at the stress s.  Returns false when a resolved-shear ratio is too large
+// at the stress s, from the staged column st.  Returns false when a resolved-shear ratio is too large
 // for |r|^n in single precision, or not finite.
-__device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, long long v, const float *s,
+__device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, const float *st, const float *s,
                                               float *edot, float *D)
 {
-    const long long nv = d.nv;
 #pragma unroll
     for (int i = 0; i < 5; ++i) edot[i] = 0.0f;
 #pragma unroll
@@ -327,10 +337,10 @@ __device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, long long v, con
     for (int k = 0; k < d.nsys; ++k) {
         float sc[5];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch32 + (long long)(5 * k + i) * nv + v);
+        for (int i = 0; i < 5; ++i) sc[i] = st[(5 * k + i) * VOCE_NR_THREADS];
         const float rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
         const int neg = rss < 0.0f;
-        const float it = __ldg(d.itau32 + (long long)(2 * k + neg) * nv + v);
+        const float it = st[(VOCE_STAGE_ITAU + 2 * k + neg) * VOCE_NR_THREADS];
         const float r = rss * it;
         const float ar = fabsf(r);
         if (!(ar < 60.0f)) return false;
@@ -347,6 +357,161 @@ __device__ __forceinline__ bool flow_rule_f32(const RveDesc &d, long long v, con
         for (int i = 0; i < 5; ++i)
 #pragma unroll
             for (int j = i; j < 5; ++j) { D[c] = fmaf(t[i], sc[j], D[c]); ++c; }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Float-float arithmetic for the mixed Newton's acceptance residual.  A value
+// is the unevaluated sum h + l of two floats, about 48 significant bits.  The
+// error-free transformations are Knuth's TwoSum and the FMA TwoProduct; the
+// dot products accumulate as in Ogita, Rump and Oishi's Dot2 ("Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26, 2005).  Each step is written in
+// the order it must be evaluated (no fast-math, nothing reassociated).  The
+// residual only needs an absolute error far below 2^-24 of its largest term,
+// so pairs are renormalised only where a product follows.
+// ---------------------------------------------------------------------------
+struct ff32 {
+    float h, l;
+};
+
+// stores x as the float pair hi[i] + lo[i]
+__device__ __forceinline__ void put_pair(float *hi, float *lo, long long i, double x)
+{
+    const float h = (float)x;
+    hi[i] = h;
+    lo[i] = (float)(x - (double)h);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// h + l with |l| below half an ulp of h (|h| >= |l| on entry)
+__device__ __forceinline__ ff32 ff_norm(float h, float l)
+{
+    ff32 r;
+    r.h = h + l;
+    r.l = l - (r.h - h);
+    return r;
+}
+
+// acc += (ah + al) * x
+__device__ __forceinline__ void ff_acc(ff32 &acc, float ah, float al, float x)
+{
+    const float p = ah * x;
+    const float pe = fmaf(ah, x, -p);
+    float s, e;
+    two_sum(acc.h, p, s, e);
+    acc.h = s;
+    acc.l += e + fmaf(al, x, pe);
+}
+
+// acc += (ah + al) * (bh + bl)
+__device__ __forceinline__ void ff_acc2(ff32 &acc, float ah, float al, float bh, float bl)
+{
+    const float p = ah * bh;
+    const float pe = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -p)));
+    float s, e;
+    two_sum(acc.h, p, s, e);
+    acc.h = s;
+    acc.l += e + pe;
+}
+
+__device__ __forceinline__ ff32 ff_mul(ff32 a, float bh, float bl)
+{
+    const float p = a.h * bh;
+    return ff_norm(p, fmaf(a.h, bl, fmaf(a.l, bh, fmaf(a.h, bh, -p))));
+}
+
+__device__ __forceinline__ ff32 ff_add(ff32 a, ff32 b)
+{
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return ff_norm(s, e + (a.l + b.l));
+}
+
+// a^e for a float pair a >= 0 and an integer e >= 1, by binary powering
+__device__ __forceinline__ ff32 ff_ipow(ff32 a, int e)
+{
+    if (e == 20) {   // a^16 a^4
+        ff32 a2 = ff_mul(a, a.h, a.l), a4 = ff_mul(a2, a2.h, a2.l);
+        ff32 a8 = ff_mul(a4, a4.h, a4.l), a16 = ff_mul(a8, a8.h, a8.l);
+        return ff_mul(a16, a4.h, a4.l);
+    }
+    ff32 res, b = a;
+    res.h = 1.0f;
+    res.l = 0.0f;
+    while (e) {
+        if (e & 1) res = ff_mul(res, b.h, b.l);
+        e >>= 1;
+        if (e) b = ff_mul(b, b.h, b.l);
+    }
+    return res;
+}
+
+// The Newton residual of evolution.c:78-83 in the symmetric form used here,
+//   x = cc + dt * edot(s) + (S_g + S0) s,
+// at a single-precision stress s, in float-float: every model quantity is
+// taken as its float pair (Schmid vectors, 1/CRSS, S_g + S0, gam0, dt), which
+// is its double value to about 2^-48, so x is the double-precision residual.
+// Ph holds the high halves of S_g + S0 (already loaded), st the staged
+// column of the high halves of the Schmid vectors and 1/CRSS (flow_rule_f32).
+// Returns false when a resolved-shear ratio leaves the single-precision range.
+__device__ __forceinline__ bool residual_ff(const RveDesc &d, long long v, const float *st,
+                                            const float (&s)[6], const double (&cc)[6],
+                                            const float (&Ph)[21], float (&x)[6])
+{
+    const long long nv = d.nv;
+    ff32 ed[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) { ed[i].h = 0.0f; ed[i].l = 0.0f; }
+    const bool uni = d.gam0_uniform != 0;
+#pragma unroll kSysUnroll
+    for (int k = 0; k < d.nsys; ++k) {
+        float sh[5], sl[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            sh[i] = st[(5 * k + i) * VOCE_NR_THREADS];
+            sl[i] = __ldg(d.sch_lo + (long long)(5 * k + i) * nv + v);
+        }
+        ff32 rss;
+        rss.h = 0.0f;
+        rss.l = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) ff_acc(rss, sh[i], sl[i], s[i]);
+        rss = ff_norm(rss.h, rss.l);
+        const int neg = rss.h < 0.0f;
+        const float ih = st[(VOCE_STAGE_ITAU + 2 * k + neg) * VOCE_NR_THREADS];
+        ff32 a = ff_mul(rss, ih, __ldg(d.itau_lo + (long long)(2 * k + neg) * nv + v));
+        if (neg) { a.h = -a.h; a.l = -a.l; }
+        if (!(a.h < 60.0f)) return false;
+        ff32 g = ff_ipow(a, d.ipow_n);   // |r|^n
+        if (!uni) g = ff_mul(g, d.gam0f[k], d.gam0l[k]);
+        if (neg) { g.h = -g.h; g.l = -g.l; }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) ff_acc2(ed[i], sh[i], sl[i], g.h, g.l);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const float ch = (float)cc[i];
+        ff32 t;
+        t.h = ch;
+        t.l = (float)(cc[i] - (double)ch);
+        if (i < 5) {
+            ff32 e = ff_norm(ed[i].h, ed[i].l);
+            if (uni) e = ff_mul(e, d.gam0f[0], d.gam0l[0]);
+            t = ff_add(t, ff_mul(e, d.dth, d.dtl));
+        }
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const int q = sym6(i, j);
+            ff_acc(t, Ph[q], __ldg(d.sgp_lo + (long long)q * nv + v), s[j]);
+        }
+        x[i] = t.h + t.l;
     }
     return true;
 }

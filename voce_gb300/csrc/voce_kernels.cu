@@ -137,7 +137,7 @@ __device__ void schmid_from_tm(const RveDesc &d, long long v, const double (&T)[
             double acc = 0.0;
             for (int c = 0; c < 5; ++c) acc += Mr[i][c] * d.schxt[5 * s + c];
             d.sch[(long long)(5 * s + i) * d.nv + v] = acc;
-            if (d.sch32) d.sch32[(long long)(5 * s + i) * d.nv + v] = (float)acc;
+            if (d.sch32) put_pair(d.sch32, d.sch_lo, (long long)(5 * s + i) * d.nv + v, acc);
         }
 }
 
@@ -177,10 +177,10 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             for (int c = 0; c < 21; ++c) d.sg[c * nv + v] = 0.0;
             for (int c = 0; c < 60; ++c) d.sch[c * nv + v] = 0.0;
             if (d.sch32)
-                for (int c = 0; c < 60; ++c) d.sch32[c * nv + v] = 0.0f;
+                for (int c = 0; c < 60; ++c) { d.sch32[c * nv + v] = 0.0f; d.sch_lo[c * nv + v] = 0.0f; }
             for (int c = 0; c < 24; ++c) { d.crss[c * nv + v] = 0.0; d.itau[c * nv + v] = 0.0; }
             if (d.itau32)
-                for (int c = 0; c < 24; ++c) d.itau32[c * nv + v] = 0.0f;
+                for (int c = 0; c < 24; ++c) { d.itau32[c * nv + v] = 0.0f; d.itau_lo[c * nv + v] = 0.0f; }
             continue;
         }
         acc[0] += 1.0;
@@ -225,8 +225,8 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             d.itau[(2 * k) * nv + v] = 1.0 / d.tau0[k];
             d.itau[(2 * k + 1) * nv + v] = 1.0 / d.tau0b[k];
             if (d.itau32) {
-                d.itau32[(2 * k) * nv + v] = (float)(1.0 / d.tau0[k]);
-                d.itau32[(2 * k + 1) * nv + v] = (float)(1.0 / d.tau0b[k]);
+                put_pair(d.itau32, d.itau_lo, (2 * k) * nv + v, 1.0 / d.tau0[k]);
+                put_pair(d.itau32, d.itau_lo, (2 * k + 1) * nv + v, 1.0 / d.tau0b[k]);
             }
         }
         double T[3][3];
@@ -475,6 +475,19 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
 // the FP64 Newton of the reference, for the FP64 and VOCE_PREC_MIXED forms.
 // ---------------------------------------------------------------------------
 
+// 4-byte asynchronous global -> shared copy (cp.async, cached in L1 and L2),
+// and the wait for all of this thread's outstanding ones
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // P = S_g + S0 (packed upper triangle) of voxel v
 __device__ __forceinline__ void load_P(const RveDesc &d, long long v, double (&P)[21])
 {
@@ -579,44 +592,12 @@ __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const
     }
 }
 
-// Strain rate only, in double precision, for the mixed form's residual: the
-// flow rule with |r|^n sign(r) formed as copysign(r^n, r) (n = 20: r^20 by
-// four squarings and one product) and gam0 taken out of the sum when all
-// systems share it.
-__device__ __forceinline__ void edot_fp64(const RveDesc &d, long long v, const double *s, double *edot)
-{
-    const long long nv = d.nv;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) edot[i] = 0.0;
-    const bool n20 = d.ipow_n == 20, uni = d.gam0_uniform != 0;
-#pragma unroll kSysUnroll
-    for (int k = 0; k < d.nsys; ++k) {
-        double sc[5];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
-        const double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
-        const int neg = rss < 0.0;
-        const double r = rss * __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
-        double g;
-        if (n20) {
-            const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8;
-            g = copysign(r16 * r4, r);
-        } else {
-            g = pow_abs_e(fabs(r), d.ipow_n - 1) * r;
-        }
-        if (!uni) g *= d.gam0[k];
-#pragma unroll
-        for (int i = 0; i < 5; ++i) edot[i] = fma(sc[i], g, edot[i]);
-    }
-    if (uni) {
-#pragma unroll
-        for (int i = 0; i < 5; ++i) edot[i] *= d.gam0[0];
-    }
-}
-
 // Mixed form: Newton in single precision (residual, Jacobian and solve) down
 // to a relative update of 1e-4, then one Newton step on the double-precision
-// residual with the last single-precision matrix.  That step is accepted when
+// residual with the last single-precision matrix.  That residual is evaluated
+// in float-float on the FP32 pipe (residual_ff), from float pairs of the
+// model data: the double-precision model to about 2^-48, at a fraction of the
+// cost of FP64 arithmetic on this part.  That step is accepted when
 // its relative update is below 1e-5: Newton's quadratic term then puts the
 // next update near 1e-9, under the 1e-7 test of the FP64 form, so the
 // accepted stress is taken as the converged point (zero residual, and the
@@ -626,10 +607,10 @@ __device__ __forceinline__ void edot_fp64(const RveDesc &d, long long v, const d
 // increment) the single-precision Newton runs down to 1e-5 and its point is
 // taken as converged: its error, a few 1e-6 relative, is far below the
 // change such an iteration makes.
-__device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, const double (&lam)[6],
-                                             const double (&cc)[6], double sn2, bool polish,
-                                             double (&sig)[6], double (&sp)[6], double (&Rl)[6],
-                                             int &it)
+__device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, const float *st,
+                                             const double (&lam)[6], const double (&cc)[6], double sn2,
+                                             bool polish, double (&sig)[6], double (&sp)[6],
+                                             double (&Rl)[6], int &it)
 {
     const double dt = d.dt;
     bool done = false;
@@ -645,10 +626,11 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
         const float thr32 = (float)((polish ? 1e-8 : 1e-10) * sn2);
         const float dtf = (float)dt;
         bool ok = true, conv = false;
+        cp_async_wait_all();   // the staged column of this voxel
         while (it < 24) {
             ++it;
             float ed[5], D[15], x[6];
-            if (!flow_rule_f32(d, v, sf, ed, D)) { ok = false; break; }
+            if (!flow_rule_f32(d, st, sf, ed, D)) { ok = false; break; }
 #pragma unroll
             for (int i = 0; i < 6; ++i) {
                 float t = ccf[i] + (i < 5 ? dtf * ed[i] : 0.0f);
@@ -676,38 +658,24 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
 #pragma unroll
             for (int c = 0; c < 6; ++c) { sig[c] = (double)sf[c]; sp[c] = sig[c]; Rl[c] = 0.0; }
         } else if (ok && conv) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c];
             ++it;
-            double ed[5];
-            edot_fp64(d, v, sig, ed);
-            double P[21];
-            reload_P(d, v, P);
             float x[6];
+            if (residual_ff(d, v, st, sf, cc, Pf, x)) {
+                ldlt_solve6f(Mf, x);
+                float dn = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                double t = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+                for (int c = 0; c < 6; ++c) {
+                    dn = fmaf(x[c], x[c], dn);
+                    sig[c] = (double)sf[c] - (double)x[c];
+                }
+                if (dn <= (float)(1e-10 * sn2)) {
+                    done = true;
 #pragma unroll
-                for (int j = 0; j < 6; ++j) t = fma(P[sym6(i, j)], sig[j], t);
-                Rl[i] = t;
-                x[i] = (float)t;
-            }
-            ldlt_solve6f(Mf, x);
-            double cnr = 0.0;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const double sn = sig[c] - (double)x[c];
-                const double dd = sn - sig[c];
-                cnr = fma(dd, dd, cnr);
-                sig[c] = sn;
-            }
-            if (cnr <= 1e-10 * sn2) {
-                done = true;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) { sp[c] = sig[c]; Rl[c] = 0.0; }
+                    for (int c = 0; c < 6; ++c) { sp[c] = sig[c]; Rl[c] = 0.0; }
+                }
             } else {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) sp[c] = (double)sf[c];
+                for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c];
             }
         } else {
 #pragma unroll
@@ -727,8 +695,11 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     // per-thread sums in shared memory (one slot per thread, the same
     // additions in the same order as register accumulators) keep them out of
     // the registers the Newton loop needs
-    __shared__ double s_acc[VOCE_NPART][128];
+    __shared__ double s_acc[VOCE_NPART][VOCE_NR_THREADS];
     const int tid = threadIdx.x;
+    // NR32: this thread's column of the staged float model data
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *st = reinterpret_cast<float *>(smem_raw) + tid;
     bool polish = true;
     if (NR32) {
         const MacroDev *m = d.macro;
@@ -739,10 +710,20 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     const long long nv = d.nv;
     for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
          v += (long long)nunits * blockDim.x) {
+        if (NR32) {
+            // asynchronous copies of the voxel's float Schmid vectors and
+            // 1/CRSS; every path below waits for them before the next voxel
+#pragma unroll
+            for (int c = 0; c < VOCE_STAGE_ITAU; ++c) cp_async4(st + c * VOCE_NR_THREADS, d.sch32 + c * nv + v);
+#pragma unroll
+            for (int c = 0; c < 24; ++c)
+                cp_async4(st + (VOCE_STAGE_ITAU + c) * VOCE_NR_THREADS, d.itau32 + c * nv + v);
+        }
         const int ph = d.phase[v];
         if (!d.solid[ph]) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = 0.0; d.sigp[c * nv + v] = 0.0; }
+            if (NR32) cp_async_wait_all();
             continue;
         }
         double lam[6], cc[6];
@@ -772,7 +753,8 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
         for (int c = 0; c < 6; ++c) { sig[c] = lam[c]; sp[c] = lam[c]; Rl[c] = 0.0; }
         int it = 0;
         if (NR32) {
-            mixed_newton(d, v, lam, cc, sn2, polish, sig, sp, Rl, it);
+            mixed_newton(d, v, st, lam, cc, sn2, polish, sig, sp, Rl, it);
+            cp_async_wait_all();   // (already done unless the float phase was skipped)
         } else {
             double P[21];
             load_P(d, v, P);
@@ -1013,8 +995,8 @@ __device__ void harden_voxel(const RveDesc &d, long long v, const double *gd)
         d.itau[(2 * i) * nv + v] = 1.0 / c0;
         d.itau[(2 * i + 1) * nv + v] = 1.0 / c1;
         if (d.itau32) {
-            d.itau32[(2 * i) * nv + v] = (float)(1.0 / c0);
-            d.itau32[(2 * i + 1) * nv + v] = (float)(1.0 / c1);
+            put_pair(d.itau32, d.itau_lo, (2 * i) * nv + v, 1.0 / c0);
+            put_pair(d.itau32, d.itau_lo, (2 * i + 1) * nv + v, 1.0 / c1);
         }
     }
     d.gamacum[v] = gamtot + deltgam;
@@ -1579,8 +1561,13 @@ cudaError_t set_batch_smem(const BatchPlan &bp)
     return bp.mixed ? set_batch_smem_t<float>(bp) : set_batch_smem_t<double>(bp);
 }
 
+// dynamic shared memory of kb_nr<true>: the staged float model columns
+static const int kNrStageBytes = VOCE_STAGE_FLOATS * VOCE_NR_THREADS * (int)sizeof(float);
+
 // Newton-kernel blocks resident per GPU (SMs x blocks per SM): the grid cap
-// of kb_nr and the most units an RVE is split into for it
+// of kb_nr and the most units an RVE is split into for it.  The first call
+// also raises kb_nr<true>'s dynamic shared-memory limit; it is made when an
+// RVE is created, before any launch or stream capture.
 int nr_resident_blocks(bool nr32)
 {
     static int cached[2] = {0, 0};
@@ -1589,8 +1576,12 @@ int nr_resident_blocks(bool nr32)
         int dev = 0, sms = 152, per = 2;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (nr32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, 128, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, 128, 0);
+        if (nr32) {
+            cudaFuncSetAttribute(kb_nr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNrStageBytes);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, VOCE_NR_THREADS, kNrStageBytes);
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, VOCE_NR_THREADS, 0);
+        }
         c = sms * (per > 0 ? per : 1);
     }
     return c;
@@ -1614,7 +1605,7 @@ template <typename R>
 static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cudaGraphConditionalHandle cond,
                              int use_cond)
 {
-    const int FG = 152 * 4, NG = 152 * 2;
+    const int FG = 152 * 4;
     const RveDesc *D = bp.descs;
     pf.begin(K_FFT_Z_FWD, s);
     kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
@@ -1633,10 +1624,10 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     pf.end(K_FFT_Z_INV, s);
     pf.begin(K_NR, s);
     if (bp.nr32)
-        kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), 128, 0, s>>>(
+        kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), VOCE_NR_THREADS, kNrStageBytes, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else
-        kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), 128, 0, s>>>(
+        kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     pf.end(K_NR, s);
     pf.begin(K_FIN_ITER, s);
@@ -1837,7 +1828,7 @@ cudaError_t launch_fill_green(const RveDesc &d, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// sgp32 = (float)(S_g + S0) once S0 is known (mixed form)
+// sgp32 + sgp_lo = S_g + S0 once S0 is known (mixed form)
 __global__ void k_fill_p32(RveDesc d)
 {
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < d.nv;
@@ -1845,7 +1836,7 @@ __global__ void k_fill_p32(RveDesc d)
         double P[21];
         load_P(d, v, P);
         const bool solid = d.solid[d.phase[v]] != 0;
-        for (int q = 0; q < 21; ++q) d.sgp32[(long long)q * d.nv + v] = solid ? (float)P[q] : 0.0f;
+        for (int q = 0; q < 21; ++q) put_pair(d.sgp32, d.sgp_lo, (long long)q * d.nv + v, solid ? P[q] : 0.0);
     }
 }
 
