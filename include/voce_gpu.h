@@ -135,6 +135,20 @@ enum {
     VOCE_FIELD_RHO_RSS = 12,   /* rho_rss  (evolution.c:509-529: updated by  */
     VOCE_FIELD_RHO_CRSS = 13,  /* rho_crss  each increment from the third on */
     VOCE_FIELD_WORK_P = 14,    /* work_p    when Hard_Flag is 1; 0 before), 1 */
+    VOCE_FIELD_DISP_FLUCT = 15, /* displacement fluctuation u~ (voxel units of
+                                  length), 3: the periodic field whose gradient
+                                  is DisGrad minus its average, computed when
+                                  asked for.  It stands in for the reference's
+                                  displacement_fluct (evolution.c:532-560),
+                                  which sums over voxels into one value per
+                                  component and scales by g = xi/|xi| instead
+                                  of xi/|xi|^2.  Terms along a Nyquist
+                                  coordinate cancel, as in the Green
+                                  operator.  Allocates a 9-component spectrum
+                                  work array on first use (72 B per voxel in
+                                  FP64, 36 B in the mixed forms); single-
+                                  precision spectrum in the mixed forms.  Not
+                                  available through voce_rve_get_field_noalloc */
     VOCE_FIELD_SIG_VOIGT = 20, /* Sig 11,22,33,23,13,12: the order of the
                                   sig_1..6 dumps (io.c:321-358), 6 */
     VOCE_FIELD_EDOT_VOIGT = 21 /* Edot in the same order (io.c:360-397), 6 */

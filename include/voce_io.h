@@ -52,9 +52,13 @@ enum {
                                0.5 Sig : T(els), T() reading the Voigt-ordered
                                elastic strain as basis coefficients as the
                                reference does */
-    VOCE_IOUT_NEW_POSITION = 14 /* WriteNewPositionMPI io.c:806-858: not written
-                               (VOCE_ERR_UNSUPPORTED); the displacement field it
-                               dumps is not computed (evolution.c:532-560) */
+    VOCE_IOUT_NEW_POSITION = 14 /* WriteNewPositionMPI io.c:806-858: <name>_S%04d.iout,
+                               24-byte records of 3 doubles: the displacement
+                               fluctuation VOCE_FIELD_DISP_FLUCT.  Same names and
+                               layout as the reference's; the values are the
+                               corrected field, where the reference's
+                               (evolution.c:532-560) come out as
+                               -fluctuation[i][2] */
 };
 
 /* One dump of the RVE's current state. */
@@ -63,8 +67,8 @@ int voce_rve_write_iout(voce_rve *r, int kind, const char *name, int step);
 /* The dumps Evolution() writes after increment istep (1-based), under the
  * namelist the RVE was created from: with PrintControl[0] == 1 and istep a
  * multiple of PrintControl[1], eps, sig, els and edot, plus (Tex_Flag 1)
- * slip_sys, taux_sys, crss_sys, tex, rho_rss, rho_crss, work_p, SVM and EVM
- * (evolution.c:568-589).  Returns VOCE_OK without writing when istep is not
+ * slip_sys, taux_sys, crss_sys, tex, rho_rss, rho_crss, work_p, SVM, EVM and
+ * new_position (evolution.c:568-589).  Returns VOCE_OK without writing when istep is not
  * selected.  dir is prepended to the names ("" or NULL: current directory). */
 int voce_rve_write_step_iout(voce_rve *r, int istep, const char *dir);
 /* The final set Evolution() writes with Tex_Flag 1 (evolution.c:592-611),

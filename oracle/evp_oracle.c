@@ -1349,3 +1349,58 @@ int oracle_get_reference_medium(const oracle_job *j, double *c066, double *s066,
     if (wgt_ph1) *wgt_ph1 = j->Wgt_ph1;
     return 0;
 }
+
+/* Displacement fluctuation, the computation evolution.c:532-560 sets out to
+ * make, with its three faults corrected:
+ *   - tmp_re/tmp_im are accumulated per frequency (the reference sums them
+ *     over all voxels into one scalar per component, :545-546);
+ *   - the inverse transform is taken of that accumulated spectrum (the
+ *     reference stores the scalar at the stale index pIDX, :549-550, and
+ *     transforms what is left of the last forward transform);
+ *   - the weight is q = xi/|xi|^2, which makes the result an inverse gradient
+ *     (the reference's g, init.c:660-676, is xi/|xi|).
+ * Per component i: tmp(k) = sum_j i F^_ij(k) q_j(k), u_i = -Re(IFFT(tmp))/Nxyz,
+ * with the reference's frequencies xi (init.c:660-667) and q(0) = 0.
+ * from_fluct 1 transforms the accumulated `fluctuation` (evolution.c:392),
+ * 0 transforms DisGrad (the same spectrum away from k = 0 while DisGrad is
+ * never reset, i.e. without creep).  out: 3 doubles per voxel. */
+int oracle_disp_fluct(oracle_job *j, int from_fluct, double *out)
+{
+    const int nx = j->CellDim[0], ny = j->CellDim[1], nz = j->CellDim[2];
+    const long nv = j->nv;
+    const double *src = from_fluct ? j->fluct : j->DG;
+    double *q = (double *)malloc(sizeof(double) * 3 * (size_t)nv);
+    double *tr = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *ti = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *F = j->fft;
+    if (!q || !tr || !ti) { free(q); free(tr); free(ti); return -1; }
+    for (int x = 0; x < nx; ++x)
+        for (int y = 0; y < ny; ++y)
+            for (int z = 0; z < nz; ++z) {
+                long v = ((long)x * ny + y) * nz + z;
+                double t[3];
+                t[0] = (double)(x) * (double)(1.0 / nx);
+                t[1] = (double)(y) * (double)(1.0 / ny);
+                t[2] = (double)(z) * (double)(1.0 / nz);
+                for (int m = 0; m < 3; ++m) { t[m] -= round(t[m]); t[m] *= TWO_PI_REF; }
+                double s = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+                for (int m = 0; m < 3; ++m) q[3 * v + m] = (v == 0) ? 0.0 : t[m] / s;
+            }
+    for (int mi = 0; mi < 3; ++mi) {
+        memset(tr, 0, sizeof(double) * (size_t)nv);
+        memset(ti, 0, sizeof(double) * (size_t)nv);
+        for (int mj = 0; mj < 3; ++mj) {
+            for (long v = 0; v < nv; ++v) { F[2 * v] = src[9 * v + 3 * mi + mj]; F[2 * v + 1] = 0.0; }
+            fftc_3d(nx, ny, nz, -1, F, j->nthreads);
+            for (long v = 0; v < nv; ++v) {
+                tr[v] += -F[2 * v + 1] * q[3 * v + mj];
+                ti[v] += F[2 * v] * q[3 * v + mj];
+            }
+        }
+        for (long v = 0; v < nv; ++v) { F[2 * v] = tr[v]; F[2 * v + 1] = ti[v]; }
+        fftc_3d(nx, ny, nz, 1, F, j->nthreads);
+        for (long v = 0; v < nv; ++v) out[3 * v + mi] = -F[2 * v] / j->Nxyz;
+    }
+    free(q); free(tr); free(ti);
+    return 0;
+}

@@ -70,6 +70,10 @@ int oracle_get_iter_log(const oracle_job *j, int k, double *err_e,
 int oracle_get_field(const oracle_job *j, int id, double *out);
 long oracle_nvox(const oracle_job *j);
 int oracle_dims(const oracle_job *j, int *dims3);
+/* Displacement fluctuation (the corrected evolution.c:532-560), 3 doubles
+ * per voxel, from the accumulated fluctuation (from_fluct 1) or from DisGrad
+ * (0).  Uses the job's FFT buffer; returns 0, or -1 when out of memory. */
+int oracle_disp_fluct(oracle_job *j, int from_fluct, double *out);
 /* C066 (36), S066 (36), WGT, Wgt_ph1 */
 int oracle_get_reference_medium(const oracle_job *j, double *c066,
                                 double *s066, double *wgt_ph1);

@@ -76,6 +76,7 @@ def lib() -> C.CDLL:
         L.oracle_nvox.argtypes = [C.c_void_p]
         L.oracle_get_reference_medium.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_lu_inv66.argtypes = [C.c_void_p]
+        L.oracle_disp_fluct.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _LIB = L
     return _LIB
 
@@ -113,6 +114,14 @@ class Job:
         lib().oracle_get_field(self._h, fid, out.ctypes.data)
         return out
 
+    def disp_fluct(self, from_fluct: bool = True) -> np.ndarray:
+        """The corrected displacement fluctuation (evolution.c:532-560), from
+        the accumulated fluctuation or from DisGrad; (nv, 3)."""
+        out = np.zeros((self.nv, 3))
+        if lib().oracle_disp_fluct(self._h, 1 if from_fluct else 0, out.ctypes.data) != 0:
+            raise MemoryError("oracle_disp_fluct")
+        return out
+
     def reference_medium(self):
         c = np.zeros(36)
         s = np.zeros(36)
@@ -130,3 +139,36 @@ class Job:
             self.close()
         except Exception:
             pass
+
+
+TWO_PI_REF = 6.28318530718   # evp.h:58
+
+
+def ref_freq(n: int) -> np.ndarray:
+    """The reference's frequencies of one axis (init.c:660-667): 2 pi
+    (i/n - round(i/n)), C's round (halves away from zero, so the Nyquist
+    index of an even n gets -pi)."""
+    t = np.arange(n) * (1.0 / n)
+    r = np.floor(np.abs(t) + 0.5) * np.sign(t)
+    return (t - r) * TWO_PI_REF
+
+
+def disp_fluct_np(grad: np.ndarray, dims) -> np.ndarray:
+    """numpy form of oracle_disp_fluct: grad (nv, 9) row-major 3x3 per voxel,
+    voxels x slowest; returns (nv, 3) = -Re(IFFT(sum_j i FFT(grad_ij) q_j))/N
+    with q = xi/|xi|^2, q(0) = 0."""
+    nx, ny, nz = dims
+    g = grad.reshape(nx, ny, nz, 3, 3)
+    xi = np.meshgrid(ref_freq(nx), ref_freq(ny), ref_freq(nz), indexing="ij")
+    s = xi[0] ** 2 + xi[1] ** 2 + xi[2] ** 2
+    s[0, 0, 0] = 1.0
+    q = [x / s for x in xi]
+    for x in q:
+        x[0, 0, 0] = 0.0
+    out = np.zeros((nx, ny, nz, 3))
+    for i in range(3):
+        acc = np.zeros((nx, ny, nz), complex)
+        for j in range(3):
+            acc += 1j * np.fft.fftn(g[..., i, j]) * q[j]
+        out[..., i] = -np.fft.ifftn(acc).real
+    return out.reshape(-1, 3)

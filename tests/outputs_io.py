@@ -8,9 +8,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "outputs_tex_4x6x8.npz")
-# written by the reference but not by this library: the displacement field
-# behind them is not computed (evolution.c:532-560)
-NOT_WRITTEN = ("new_position",)
+# written by both, with values that differ on purpose: the reference's
+# displacement_fluct (evolution.c:532-560) sums over voxels into one value per
+# component and leaves the transform of the last gradient component in place,
+# while this library writes the corrected displacement fluctuation; names and
+# record sizes are compared, values are checked against the oracle instead
+VALUES_DIFFER = ("new_position",)
 # bound on every value of a dump relative to the largest magnitude in it, as
 # for the fields in the parity tests
 VALUE_TOL = 1e-9
@@ -79,13 +82,15 @@ def compare_dir(d: str, fx) -> dict:
     """Check the .iout files, vm.out and err.out in d against the fixture;
     returns a small report."""
     ours = sorted(f for f in os.listdir(d) if f.endswith(".iout"))
-    want = sorted(n for n in fx["files"] if not n.startswith(NOT_WRITTEN))
+    want = sorted(fx["files"])
     assert ours == want, (set(ours) ^ set(want))
     worst = 0.0
     for n in want:
         a = open(os.path.join(d, n), "rb").read()
         b = fx["files"][n]
         assert len(a) == len(b), n
+        if n.startswith(VALUES_DIFFER):
+            continue
         fa, ia, pa = split_records(n, a)
         fb, ib, pb = split_records(n, b)
         assert np.array_equal(ia, ib), n

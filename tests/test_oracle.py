@@ -108,3 +108,52 @@ def test_synthetic_meshes_are_reproducible():
     e = synth.so3_uniform_bunge(np.random.Generator(np.random.PCG64(0)), 20000)
     c = np.cos(np.radians(e[:, 1]))
     assert abs(c.mean()) < 0.02 and abs((c ** 2).mean() - 1 / 3) < 0.02
+
+
+def test_oracle_fluctuation_pinned_to_the_reference_new_position(oracle_lib):
+    """The reference's new_position dump (evolution.c:532-560, io.c:806-858)
+    is, because of its stale index, the inverse transform of the forward
+    transform of fluctuation[i][2]: -fluctuation[i][2] per voxel.  The
+    oracle's accumulated fluctuation reproduces the reference's own file, and
+    so does DisGrad minus its average (the fluctuation reaches DisGrad with
+    uniform terms only)."""
+    import make_outputs
+    import outputs_io
+    fx = outputs_io.load()
+    case = make_outputs.tex_case()
+    d = tempfile.mkdtemp(prefix="orc_np_")
+    nl = case.write(d, print_control=make_outputs.PRINT_CONTROL, tex_flag=make_outputs.TEX_FLAG)
+    j = orc.Job(nl)
+    j.run(3)
+    ref = np.frombuffer(fx["files"]["new_position_S0003.iout"], "<f8").reshape(-1, 3)
+    dg = j.field("disgrad").reshape(-1, 3, 3)
+    fl = dg - dg.mean(axis=0)
+    assert gio.rel(-fl[:, :, 2], ref) < 1e-12
+    # the corrected field from the accumulated fluctuation and from DisGrad
+    a = j.disp_fluct(True)
+    b = j.disp_fluct(False)
+    assert gio.rel(a, b) < 1e-12
+    assert gio.rel(b, orc.disp_fluct_np(j.field("disgrad"), case.mesh.dims)) < 1e-12
+
+
+def test_disp_fluct_known_answer():
+    """The corrected transform inverts the gradient: for a band-limited
+    periodic u (no Nyquist content), the displacement of F = grad u is u minus
+    its mean, on a grid with radix-2, -3 and -5 axes."""
+    nx, ny, nz = 8, 6, 10
+    x, y, z = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    kx, ky, kz = 2 * np.pi / nx, 2 * np.pi / ny, 2 * np.pi / nz
+    a1 = 2 * ky * y + kz * z
+    u = np.stack([np.sin(kx * x) + 0.3 * np.cos(a1), 0.5 * np.cos(kx * x + ky * y),
+                  0.2 * np.sin(3 * kz * z) + 0.1 * np.sin(kx * x)], -1)
+    F = np.zeros((nx, ny, nz, 3, 3))
+    F[..., 0, 0] = kx * np.cos(kx * x)
+    F[..., 0, 1] = -0.3 * 2 * ky * np.sin(a1)
+    F[..., 0, 2] = -0.3 * kz * np.sin(a1)
+    F[..., 1, 0] = -0.5 * kx * np.sin(kx * x + ky * y)
+    F[..., 1, 1] = -0.5 * ky * np.sin(kx * x + ky * y)
+    F[..., 2, 0] = 0.1 * kx * np.cos(kx * x)
+    F[..., 2, 2] = 0.6 * kz * np.cos(3 * kz * z)
+    got = orc.disp_fluct_np(F.reshape(-1, 9), (nx, ny, nz))
+    want = (u - u.mean(axis=(0, 1, 2))).reshape(-1, 3)
+    assert np.max(np.abs(got - want)) < 1e-12

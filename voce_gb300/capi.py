@@ -29,10 +29,10 @@ IOUT = {"eps": 0, "sig": 1, "els": 2, "edot": 3, "slip": 4, "taux": 5, "crss": 6
         "new_position": 14}
 FIELD = {"sig": 0, "eps": 1, "edot": 2, "disgrad": 3, "tranmat": 4, "crss": 5,
          "gamdot": 6, "gamacum": 7, "svm": 8, "evm": 9, "gammatotal": 10,
-         "taux": 11, "rho_rss": 12, "rho_crss": 13, "work_p": 14,
+         "taux": 11, "rho_rss": 12, "rho_crss": 13, "work_p": 14, "disp_fluct": 15,
          "sig_voigt": 20, "edot_voigt": 21}
 FIELD_WIDTH = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 12, 7: 1, 8: 1, 9: 1,
-               10: 12, 11: 12, 12: 1, 13: 1, 14: 1, 20: 6, 21: 6}
+               10: 12, 11: 12, 12: 1, 13: 1, 14: 1, 15: 3, 20: 6, 21: 6}
 
 
 class VoceNamelist(C.Structure):

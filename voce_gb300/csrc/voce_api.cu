@@ -207,6 +207,7 @@ struct voce_rve {
     std::vector<void *> dev_allocs;
     int *h_flag = nullptr;  // pinned
     double *d_out = nullptr;
+    void *d_dispwork = nullptr;   // spectrum work array of the displacement fluctuation
     double *d_flush = nullptr;
     long long flush_n = 0;
     Prof prof;
@@ -233,6 +234,7 @@ struct voce_rve {
         if (plan_maps) cudaFree(plan_maps);
         for (void *p : dev_allocs) cudaFree(p);
         if (d_out) cudaFree(d_out);
+        if (d_dispwork) cudaFree(d_dispwork);
         if (d_flush) cudaFree(d_flush);
         if (h_flag) cudaFreeHost(h_flag);
         for (int k = 0; k < 2 * K_COUNT; ++k)
@@ -1205,11 +1207,17 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out)
     case 0: case 1: case 2: case 3: case 4: per = 9; break;
     case 5: case 6: case 10: case 11: per = 12; break;
     case 7: case 8: case 9: case 12: case 13: case 14: per = 1; break;
+    case 15: per = 3; break;
     case 20: case 21: per = 6; break;
     default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
     }
     if (!r->d_out) CUDA_TRY(cudaMalloc(&r->d_out, sizeof(double) * 12 * r->d.nv));
-    CUDA_TRY(launch_field_out(r->d, field, r->d_out, r->stream));
+    if (field == VOCE_FIELD_DISP_FLUCT) {
+        if (!r->d_dispwork) CUDA_TRY(cudaMalloc(&r->d_dispwork, disp_work_bytes(r->d)));
+        CUDA_TRY(launch_disp_fluct(r->d, r->d_dispwork, r->d_out, r->stream));
+    } else {
+        CUDA_TRY(launch_field_out(r->d, field, r->d_out, r->stream));
+    }
     CUDA_TRY(cudaMemcpyAsync(host_out, r->d_out, sizeof(double) * per * r->d.nv, cudaMemcpyDeviceToHost, r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     return VOCE_OK;
@@ -1283,6 +1291,10 @@ int voce_rve_get_field_noalloc(voce_rve *r, int field, double *host_out)
     case 5: case 6: case 10: case 11: per = 12; break;
     case 7: case 8: case 9: case 12: case 13: case 14: per = 1; break;
     case 20: case 21: per = 6; break;
+    case 15:
+        return fail(VOCE_ERR_UNSUPPORTED,
+                    "field 15 (displacement fluctuation) transforms through a spectrum work array; "
+                    "use voce_rve_get_field");
     default: return fail(VOCE_ERR_ARG, "unknown field %d", field);
     }
     const long long n = (long long)per * r->d.nv;

@@ -261,8 +261,13 @@ int voce_rve_write_iout(voce_rve *r, int kind, const char *name, int step)
     case VOCE_IOUT_RHO_CRSS: return write_scalar(r, dm, VOCE_FIELD_RHO_CRSS, "%s_S%04d.iout", name, step);
     case VOCE_IOUT_WORK_P: return write_scalar(r, dm, VOCE_FIELD_WORK_P, "%s_S%06d.iout", name, step);
     case VOCE_IOUT_WORK_E: return write_work_e(r, dm, name, step);
-    case VOCE_IOUT_NEW_POSITION:
-        return fail_io(VOCE_ERR_UNSUPPORTED, "new_position: the displacement field is not computed");
+    case VOCE_IOUT_NEW_POSITION: {
+        // 24-byte records of three doubles (io.c:806-858), here the corrected
+        // displacement fluctuation (VOCE_FIELD_DISP_FLUCT)
+        std::vector<double> f;
+        if ((rc = get(r, VOCE_FIELD_DISP_FLUCT, 3 * dm.nv, f))) return rc;
+        return write_file(fmt_name("%s_S%04d.iout", name, step), f.data(), sizeof(double) * 3 * dm.nv);
+    }
     default: return fail_io(VOCE_ERR_ARG, "unknown .iout kind " + std::to_string(kind));
     }
 }
@@ -282,7 +287,8 @@ int voce_rve_write_step_iout(voce_rve *r, int istep, const char *dir)
     static const struct { int kind; const char *name; } tex[] = {
         {VOCE_IOUT_SLIP, "slip_sys"}, {VOCE_IOUT_TAUX, "taux_sys"}, {VOCE_IOUT_CRSS, "crss_sys"},
         {VOCE_IOUT_TEX, "tex"}, {VOCE_IOUT_RHO_RSS, "rho_rss"}, {VOCE_IOUT_RHO_CRSS, "rho_crss"},
-        {VOCE_IOUT_WORK_P, "work_p"}, {VOCE_IOUT_SVM, "SVM"}, {VOCE_IOUT_EVM, "EVM"}};
+        {VOCE_IOUT_WORK_P, "work_p"}, {VOCE_IOUT_SVM, "SVM"}, {VOCE_IOUT_EVM, "EVM"},
+        {VOCE_IOUT_NEW_POSITION, "new_position"}};
     for (const auto &w : base)
         if ((rc = voce_rve_write_iout(r, w.kind, join(dir, w.name).c_str(), istep))) return rc;
     if (nl.Tex_Flag == 1)
@@ -302,7 +308,8 @@ int voce_rve_write_final_iout(voce_rve *r, const char *dir)
         {VOCE_IOUT_TEX, "tex_final"}, {VOCE_IOUT_SVM, "SVM_final"}, {VOCE_IOUT_EVM, "EVM_final"},
         {VOCE_IOUT_RHO_RSS, "rho_rss_final"}, {VOCE_IOUT_RHO_CRSS, "rho_crss_final"},
         {VOCE_IOUT_WORK_P, "work_p_final"}, {VOCE_IOUT_WORK_E, "work_e_final"},
-        {VOCE_IOUT_EPS, "eps_final"}, {VOCE_IOUT_SIG, "sig_final"}, {VOCE_IOUT_EDOT, "edot_final"},
+        {VOCE_IOUT_EPS, "eps_final"}, {VOCE_IOUT_SIG, "sig_final"},
+        {VOCE_IOUT_NEW_POSITION, "new_position_final"}, {VOCE_IOUT_EDOT, "edot_final"},
         {VOCE_IOUT_ELS, "els_final"}};
     for (const auto &w : fin)
         if ((rc = voce_rve_write_iout(r, w.kind, join(dir, w.name).c_str(), 0))) return rc;

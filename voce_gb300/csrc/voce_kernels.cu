@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
 // ---------------------------------------------------------------------------
 // FFT passes
 // ---------------------------------------------------------------------------
+// the stress's six components into the spectrum (evolution.c:350-361)
 template <typename R>
 __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
 {
@@ -288,6 +289,50 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
         spec[(long long)(2 * p + 1) * nzh * plane + o] = B;
     }
 }
+
+
+// forward r2c along z of ncomp real fields src[c][nv] into the half
+// spectrum dstp[c][nzh][nx][ny]: two fields per complex line (an odd count
+// pads the last line with zeros), split by the Hermitian symmetry of each
+template <typename R, int ncomp>
+__device__ void fft_z_fwd_src(const RveDesc &d, const double *src, void *dstp, int rows, int unit)
+{
+    typedef typename Cx<R>::T C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *bufA = reinterpret_cast<C *>(smem_raw);
+    const int nx = d.nx, ny = d.ny, nz = d.nz, nzh = d.nzh;
+    const long long nv = d.nv;
+    const int np = (ncomp + 1) / 2;
+    const int NL = np * rows, ldl = NL | 1;
+    C *bufB = bufA + nz * ldl;
+    const int ytiles = ny / rows;
+    const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
+    const long long vb = ((long long)x * ny + y0) * nz;
+    for (int idx = threadIdx.x; idx < 2 * np * rows * nz; idx += blockDim.x) {
+        const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+        const R val = (ncomp % 2 == 0 || c < ncomp) ? (R)__ldg(src + c * nv + vb + (long long)r * nz + z) : R(0);
+        C *e = &bufA[z * ldl + (c >> 1) * rows + r];
+        if (c & 1) e->y = val; else e->x = val;
+    }
+    __syncthreads();
+    C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, -1);
+    C *spec = (C *)dstp;
+    const long long plane = (long long)nx * ny;
+    for (int idx = threadIdx.x; idx < np * rows * nzh; idx += blockDim.x) {
+        const int r = idx % rows, t = idx / rows, k = t % nzh, p = t / nzh;
+        const int l = p * rows + r;
+        const C zk = res[k * ldl + l], zm = res[((nz - k) % nz) * ldl + l];
+        C A, B;
+        A.x = R(0.5) * (zk.x + zm.x);
+        A.y = R(0.5) * (zk.y - zm.y);
+        B.x = R(0.5) * (zk.y + zm.y);
+        B.y = R(-0.5) * (zk.x - zm.x);
+        const long long o = (long long)k * plane + (long long)x * ny + y0 + r;
+        spec[(long long)(2 * p) * nzh * plane + o] = A;
+        if (ncomp % 2 == 0 || 2 * p + 1 < ncomp) spec[(long long)(2 * p + 1) * nzh * plane + o] = B;
+    }
+}
+
 
 
 template <typename R>
@@ -408,9 +453,11 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
 
 // inverse z transform (Hermitian half spectrum -> real); mode 0 adds the
 // result to the symmetric displacement gradient (evolution.c:383-394),
-// mode 1 writes it (scaled by 1/N) to rotl
+// mode 1 writes it (scaled by 1/N) to rotl, mode 2 (scaled by 1/N) to
+// out[ncomp * v + c], voxel by voxel
 template <typename R>
-__device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int rows, int mode, int unit)
+__device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int rows, int mode, int unit,
+                               double *out = nullptr)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -455,12 +502,19 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
             const long long g = (long long)c * nv + vb + (long long)r * nz + z;
             d.dgs[g] += m->ddg6[c] + val * inv;
         }
-    } else {
+    } else if (mode == 1) {
         for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x) {
             const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
             const C e = res[z * ldl + (c >> 1) * rows + r];
             const double val = (double)((c & 1) ? e.y : e.x);
             d.rotl[(long long)c * nv + vb + (long long)r * nz + z] = val * inv;
+        }
+    } else {
+        for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x) {
+            const int c = idx % ncomp, t = idx / ncomp, z = t % nz, r = t / nz;
+            const C e = res[z * ldl + (c >> 1) * rows + r];
+            const double val = (double)((c & 1) ? e.y : e.x);
+            out[ncomp * (vb + (long long)r * nz + z) + c] = val * inv;
         }
     }
 }
@@ -1909,6 +1963,160 @@ double measure_fp64_tflops()
     cudaFree(out);
     const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
     return ms > 0.f ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Displacement fluctuation: the periodic field u~ whose gradient is the
+// fluctuating part of DisGrad, in voxel units of length.  The reference means
+// to compute it at evolution.c:532-560 from
+//   u^_i(k) = -i sum_j F^_ij(k) g_j(k),   u~ = Re(IFFT(u^)) / N
+// but sums tmp_re/tmp_im into one scalar per component over all voxels, then
+// stores it at a stale voxel index, and its g = xi/|xi| (init.c:660-676)
+// lacks the 1/|xi| an inverse gradient needs.  Here F is DisGrad (its
+// fluctuating part is the reference's `fluctuation`, evolution.c:392, up to
+// the uniform terms that only reach k = 0), g_j = xi_j/|xi|^2 with the
+// reference's frequencies xi, g(0) = 0, and the real part is taken the way
+// the Green operator takes it: the spectrum is replaced by its Hermitian part
+// (X(k) + conj X(-k))/2, which turns g into (g(k) - g(-k))/2 and cancels the
+// terms along a Nyquist coordinate.  The work array holds [9][nzh][nx][ny]
+// complex values of the spectrum type: DisGrad's six B-basis symmetric
+// components, then its three antisymmetric ones.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void freq_over_sq(const RveDesc &d, int ix, int iy, int iz, double (&q)[3])
+{
+    const double g0 = kfreq(ix, d.inv_n[0]), g1 = kfreq(iy, d.inv_n[1]), g2 = kfreq(iz, d.inv_n[2]);
+    const double s = 1.0 / (g0 * g0 + g1 * g1 + g2 * g2);
+    q[0] = g0 * s; q[1] = g1 * s; q[2] = g2 * s;
+}
+
+// which 0: the symmetric part into components 0-5; 1: the antisymmetric
+// part into 6-8
+template <typename R>
+__global__ void __launch_bounds__(256) k_disp_z_fwd(RveDesc d, void *work, int which, int total)
+{
+    typedef typename Cx<R>::T C;
+    C *anti = (C *)work + 6 * d.nspec;
+    for (int u = blockIdx.x; u < total; u += gridDim.x) {
+        if (which == 0) fft_z_fwd_src<R, 6>(d, d.dgs, work, d.zrows, u);
+        else fft_z_fwd_src<R, 3>(d, d.dga, anti, d.zirows3, u);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_disp_fft_y(RveDesc d, void *work, int sign, int total)
+{
+    for (int u = blockIdx.x; u < total; u += gridDim.x) {
+        fft_y_unit<R>(d, work, sign, d.yxt, u);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_disp_fft_x(RveDesc d, void *work, int ncomp, int sign, int kc, int total)
+{
+    for (int u = blockIdx.x; u < total; u += gridDim.x) {
+        fft_x_unit<R>(d, work, ncomp, sign, kc, u);
+        __syncthreads();
+    }
+}
+
+// per frequency: the nine transformed components -> u^ in components 0-2
+template <typename R>
+__global__ void __launch_bounds__(256) k_disp_spec(RveDesc d, void *work)
+{
+    typedef typename Cx<R>::T C;
+    C *w = (C *)work;
+    const long long ns = d.nspec, plane = (long long)d.nx * d.ny;
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < ns;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(o / plane), ix = (int)((o % plane) / d.ny), iy = (int)(o % d.ny);
+        double q[3] = {0.0, 0.0, 0.0};
+        if ((ix | iy | iz) != 0) {
+            double a[3], b[3];
+            freq_over_sq(d, ix, iy, iz, a);
+            freq_over_sq(d, (d.nx - ix) % d.nx, (d.ny - iy) % d.ny, (d.nz - iz) % d.nz, b);
+            for (int m = 0; m < 3; ++m) q[m] = 0.5 * (a[m] - b[m]);
+        }
+        double br[6], bi[6], Fr[9], Fi[9];
+        for (int c = 0; c < 6; ++c) {
+            const C e = w[c * ns + o];
+            br[c] = (double)e.x;
+            bi[c] = (double)e.y;
+        }
+        sym9_from_b(br, Fr);
+        sym9_from_b(bi, Fi);
+        // antisymmetric parts (D12-D21)/2, (D02-D20)/2, (D01-D10)/2
+        const int ij[3] = {5, 2, 1}, ji[3] = {7, 6, 3};
+        for (int c = 0; c < 3; ++c) {
+            const C e = w[(6 + c) * ns + o];
+            Fr[ij[c]] += (double)e.x; Fr[ji[c]] -= (double)e.x;
+            Fi[ij[c]] += (double)e.y; Fi[ji[c]] -= (double)e.y;
+        }
+        for (int i = 0; i < 3; ++i) {
+            double ur = 0.0, ui = 0.0;   // -i (Fr + i Fi) q = Fi q - i Fr q
+            for (int j = 0; j < 3; ++j) {
+                ur = fma(Fi[3 * i + j], q[j], ur);
+                ui = fma(-Fr[3 * i + j], q[j], ui);
+            }
+            C e;
+            e.x = (R)ur;
+            e.y = (R)ui;
+            w[i * ns + o] = e;
+        }
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_disp_z_inv(RveDesc d, void *work, double *out, int total)
+{
+    for (int u = blockIdx.x; u < total; u += gridDim.x) {
+        fft_z_inv_unit<R>(d, work, 3, d.zirows3, 2, u, out);
+        __syncthreads();
+    }
+}
+
+template <typename R>
+static cudaError_t disp_fluct_t(const RveDesc &d, void *work, double *out, cudaStream_t s)
+{
+    const int FG = 152 * 4;
+    const int budget = (sizeof(R) == 8) ? 2048 : 4096;
+    const int kc9 = pick_div<R>(d.ny, (budget * 3 / 2) / (9 * d.nx));
+    const int xt = d.nx / d.yxt, nzh = d.nzh;
+    const size_t sz = std::max(smem_lines<R>(d.nz, 3 * d.zrows), smem_lines<R>(d.nz, 2 * d.zirows3));
+    const size_t sy = smem_lines<R>(d.ny, d.yxt);
+    const size_t sx = std::max(smem_lines<R>(d.nx, 9 * kc9), smem_lines<R>(d.nx, 3 * d.xkc3));
+    const size_t si = smem_lines<R>(d.nz, 2 * d.zirows3);
+    cudaFuncSetAttribute(k_disp_z_fwd<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+    cudaFuncSetAttribute(k_disp_fft_y<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy);
+    cudaFuncSetAttribute(k_disp_fft_x<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
+    cudaFuncSetAttribute(k_disp_z_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)si);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int uz6 = d.nx * (d.ny / d.zrows), uz3 = d.nx * (d.ny / d.zirows3);
+    k_disp_z_fwd<R><<<grid_for(uz6, FG), 256, smem_lines<R>(d.nz, 3 * d.zrows), s>>>(d, work, 0, uz6);
+    k_disp_z_fwd<R><<<grid_for(uz3, FG), 256, smem_lines<R>(d.nz, 2 * d.zirows3), s>>>(d, work, 1, uz3);
+    const int uy9 = 9 * nzh * xt, uy3 = 3 * nzh * xt;
+    k_disp_fft_y<R><<<grid_for(uy9, FG), 256, sy, s>>>(d, work, -1, uy9);
+    const int ux9 = nzh * (d.ny / kc9), ux3 = nzh * (d.ny / d.xkc3);
+    k_disp_fft_x<R><<<grid_for(ux9, FG), 256, smem_lines<R>(d.nx, 9 * kc9), s>>>(d, work, 9, -1, kc9, ux9);
+    int blocks = (int)((d.nspec + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_disp_spec<R><<<blocks, 256, 0, s>>>(d, work);
+    k_disp_fft_x<R><<<grid_for(ux3, FG), 256, smem_lines<R>(d.nx, 3 * d.xkc3), s>>>(d, work, 3, +1, d.xkc3, ux3);
+    k_disp_fft_y<R><<<grid_for(uy3, FG), 256, sy, s>>>(d, work, +1, uy3);
+    k_disp_z_inv<R><<<grid_for(uz3, FG), 256, si, s>>>(d, work, out, uz3);
+    return cudaGetLastError();
+}
+
+size_t disp_work_bytes(const RveDesc &d)
+{
+    return (size_t)9 * (size_t)d.nspec * (d.mixed ? sizeof(float2) : sizeof(double2));
+}
+
+cudaError_t launch_disp_fluct(const RveDesc &d, void *work, double *out, cudaStream_t s)
+{
+    return d.mixed ? disp_fluct_t<float>(d, work, out, s) : disp_fluct_t<double>(d, work, out, s);
 }
 
 cudaError_t launch_field_out(const RveDesc &d, int field, double *out, cudaStream_t s)

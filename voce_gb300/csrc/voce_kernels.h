@@ -101,5 +101,9 @@ double measure_fp64_tflops();
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s);
 cudaError_t launch_field_out(const RveDesc &d, int field, double *out, cudaStream_t s);
+// displacement fluctuation of d's DisGrad into out[3 * v + i], through a work
+// array of disp_work_bytes(d) (its contents on entry do not matter)
+size_t disp_work_bytes(const RveDesc &d);
+cudaError_t launch_disp_fluct(const RveDesc &d, void *work, double *out, cudaStream_t s);
 
 }  // namespace voce
