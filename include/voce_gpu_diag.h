@@ -68,6 +68,25 @@ int voce_rve_get_tiles(const voce_rve *r, int tiles[6]);
  * ny; all phases fit in shared memory); between calls, outside a batch. */
 int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
 
+/* FFT radix schedules (no counterpart in the reference, which leaves its
+ * transforms to FFTW).  Each axis of length L = 2^a 3^b runs as Stockham
+ * passes of radix 4, 2 and 3; the candidate schedules are their stage orders
+ * 4s-2-3s (the default), 3s-4s-2, 2-4s-3s and 3s-2-4s, duplicates dropped.
+ * With tuning on, voce_rve_create times the candidates of each axis on the
+ * forward pass that transforms it (with the tuned tile) and keeps one only
+ * when it is more than 3 % faster than the default; the choice is cached
+ * with the tiles (and in VOCE_TILE_CACHE).  Unlike the tiles, the schedule
+ * changes results in the last bits (a different order of roundings); an RVE
+ * keeps its schedule for life, in a batch and through snapshots.
+ * voce_fft_schedule_count: candidates for length L (0 if not 2^a 3^b).
+ * voce_rve_get_fft_schedule: the radices of axis (0 x, 1 y, 2 z) in stage
+ * order; returns the number of stages (at most max written), < 0 on error.
+ * voce_rve_set_fft_schedule: use candidate k of axis; between calls,
+ * outside a batch. */
+int voce_fft_schedule_count(int L);
+int voce_rve_get_fft_schedule(const voce_rve *r, int axis, int *radices, int max);
+int voce_rve_set_fft_schedule(voce_rve *r, int axis, int k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -152,3 +152,14 @@ def test_mesh_reader_parses_like_strtod_on_every_format(voce_lib):
     with pytest.raises(capi.VoceError) as ei:
         capi.read_mesh(path, dims)
     assert ei.value.code == 3
+
+
+def test_fft_schedule_candidates(voce_lib):
+    """Radix schedules per axis length (host only): the stage orders of the
+    radix-4/2/3 passes, duplicates dropped; lengths other than 2^a 3^b have
+    none."""
+    lib = capi.load()
+    want = {2: 1, 4: 1, 6: 2, 8: 2, 12: 2, 16: 1, 24: 4, 32: 2, 48: 2, 64: 1, 96: 4, 128: 2,
+            256: 1, 384: 4, 5: 0, 10: 0, 1: 0}
+    for n, c in want.items():
+        assert lib.voce_fft_schedule_count(n) == c, n

@@ -73,3 +73,62 @@ def test_tile_cache_file_is_shared_between_processes(voce_lib):
     b = subprocess.run([sys.executable, "-c", prog], env=env, capture_output=True, text=True, check=True)
     assert a.stdout == b.stdout
     assert open(cache).read().count("\n") == 1
+
+
+def _box_case(dims, seed):
+    return synth.Case("box_%d_%d_%d" % tuple(dims), synth.voronoi_mesh_box(dims, 10, seed),
+                      synth.CU_LIKE, synth.tension_z(), 0.2, 1)
+
+
+def test_fft_schedules_agree_and_stay_with_the_rve(voce_lib):
+    """Every radix schedule of a 24 x 32 x 48 grid (x: 4 candidates, y and z:
+    2 each) gives the default's increment to rounding: the same iteration
+    count, stress within 1e-12.  A forced schedule survives a snapshot and
+    joins a batch unchanged (the batch member's increment is bit-identical to
+    the lone run with that schedule)."""
+    case = _box_case((24, 32, 48), 84)
+    nl = case.write(tempfile.mkdtemp(prefix="sched_"))
+    lib = capi.load()
+    counts = [lib.voce_fft_schedule_count(n) for n in (24, 32, 48)]
+    assert counts == [4, 2, 2]
+
+    def run(axis=None, k=0):
+        with capi.Rve.from_files(nl) as r:
+            if axis is not None:
+                r.set_fft_schedule(axis, k)
+            sched = [r.fft_schedule(a) for a in range(3)]
+            r.run(1)
+            return sched, r.increment(0), r.field("sig_voigt")
+
+    with capi.Rve.from_files(nl) as r:
+        for a in range(3):
+            r.set_fft_schedule(a, 0)
+        r.run(1)
+        base = r.increment(0), r.field("sig_voigt")
+    seen = set()
+    for axis, n in enumerate(counts):
+        for k in range(n):
+            sched, inc, sig = run(axis, k)
+            seen.add(tuple(sched[axis]))
+            assert inc["iters"] == base[0]["iters"]
+            e = np.max(np.abs(sig - base[1])) / np.max(np.abs(base[1]))
+            assert e < 1e-12, (axis, k, sched, e)
+    assert len(seen) == sum(counts)
+    # a forced schedule is part of the RVE: snapshot and batch keep it
+    with capi.Rve.from_files(nl) as r:
+        r.set_fft_schedule(0, 2)
+        want = r.fft_schedule(0)
+        assert want == [2, 4, 3]
+        blob = r.snapshot()
+        with capi.Rve.restore(blob) as q:
+            assert q.fft_schedule(0) == want
+        alone = run(0, 2)
+        with capi.Batch() as b:
+            b.add(r, 1)
+            b.run()
+        assert r.fft_schedule(0) == want
+        assert r.increment(0) == alone[1]
+        assert np.array_equal(r.field("sig_voigt"), alone[2])
+    with capi.Rve.from_files(nl) as r:
+        with pytest.raises(capi.VoceError):
+            r.set_fft_schedule(1, 2)   # 32 has two candidates

@@ -158,6 +158,9 @@ PROTOTYPES = [
     ("voce_set_autotune", C.c_int, [C.c_int]),
     ("voce_rve_get_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("voce_fft_schedule_count", C.c_int, [C.c_int]),
+    ("voce_rve_get_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]),
+    ("voce_rve_set_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("voce_server_set_quantum", C.c_int, [C.c_void_p, C.c_int]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
@@ -409,6 +412,17 @@ class Rve:
 
     def set_tiles(self, tiles) -> None:
         _check(load().voce_rve_set_tiles(self._h, (C.c_int * 6)(*tiles)))
+
+    def fft_schedule(self, axis: int) -> list:
+        """Radices of axis (0 x, 1 y, 2 z) in stage order."""
+        buf = (C.c_int * 16)()
+        n = load().voce_rve_get_fft_schedule(self._h, axis, buf, 16)
+        if n < 0:
+            _check(-n)
+        return list(buf[:n])
+
+    def set_fft_schedule(self, axis: int, k: int) -> None:
+        _check(load().voce_rve_set_fft_schedule(self._h, axis, k))
 
     def snapshot(self) -> bytes:
         """The RVE's whole state as bytes (voce_rve_snapshot)."""

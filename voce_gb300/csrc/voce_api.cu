@@ -192,6 +192,37 @@ bool fft_plan(int L, FftPlan1 &p)
     return m == 1 && L >= 2;
 }
 
+// Radix schedules of one axis: the stage orders of its radix-4, -2 and -3
+// passes the Stockham kernels can run (any order transforms correctly; the
+// order changes the strides of each pass and the rounding of the result, at
+// the last bit).  out[0] is fft_plan's 4s-2-3s; then 3s first, the lone 2
+// first, and 3s-2-4s, each kept when it differs from those before.  Returns
+// how many were written (at most max); 0 when L is not of the form 2^a 3^b.
+int fft_schedules(int L, FftPlan1 *out, int max)
+{
+    FftPlan1 base;
+    if (max < 1 || !fft_plan(L, base)) return 0;
+    int n4 = 0, n2 = 0, n3 = 0;
+    for (int k = 0; k < base.nst; ++k) (base.rad[k] == 4 ? n4 : base.rad[k] == 2 ? n2 : n3)++;
+    // orders: 0 = 4,2,3   1 = 3,4,2   2 = 2,4,3   3 = 3,2,4
+    static const int order[4][3] = {{4, 2, 3}, {3, 4, 2}, {2, 4, 3}, {3, 2, 4}};
+    int n = 0;
+    for (int o = 0; o < 4 && n < max; ++o) {
+        FftPlan1 p;
+        p.L = L;
+        p.nst = 0;
+        for (int q = 0; q < 3; ++q) {
+            const int r = order[o][q], cnt = r == 4 ? n4 : r == 2 ? n2 : n3;
+            for (int k = 0; k < cnt; ++k) p.rad[p.nst++] = r;
+        }
+        bool seen = false;
+        for (int i = 0; i < n && !seen; ++i)
+            seen = out[i].nst == p.nst && std::memcmp(out[i].rad, p.rad, sizeof(int) * p.nst) == 0;
+        if (!seen) out[n++] = p;
+    }
+    return n;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -880,19 +911,31 @@ std::mutex g_tile_mu;
 std::map<TileKey, Tiles> g_tile_cache;
 int g_autotune = 1;
 
+// schedule index k of an axis of length L (the default when out of range)
+FftPlan1 schedule_of(int L, int k)
+{
+    FftPlan1 c[4];
+    const int n = fft_schedules(L, c, 4);
+    return c[(k >= 0 && k < n) ? k : 0];
+}
+
 void apply_tiles(voce_rve *r, const Tiles &t)
 {
     r->tiles = t;
     RveDesc &d = r->d;
     d.zrows = t.zrows; d.yxt = t.yxt; d.xkc = t.xkc;
     d.xkc3 = t.xkc3; d.zirows = t.zirows; d.zirows3 = t.zirows3;
+    d.plx = schedule_of(d.nx, t.sx);
+    d.ply = schedule_of(d.ny, t.sy);
+    d.plz = schedule_of(d.nz, t.sz);
     r->plan_dirty = true;
 }
 
 // VOCE_TILE_CACHE=<file>: tile choices are read from the file before any
 // tuning and each new choice is appended, so that another process on the
 // same machine (a profiler's run of the same command, say) uses the same
-// tiles.  One line per shape: nx ny nz mixed zrows yxt xkc xkc3 zirows zirows3.
+// tiles.  One line per shape: nx ny nz mixed zrows yxt xkc xkc3 zirows
+// zirows3 sx sy sz (the last three: radix schedule indices of x, y, z).
 bool g_tile_file_read = false;
 
 void read_tile_file()
@@ -904,8 +947,8 @@ void read_tile_file()
     if (!f) return;
     TileKey k;
     Tiles t;
-    while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d", &k.nx, &k.ny, &k.nz, &k.mixed, &t.zrows, &t.yxt,
-                       &t.xkc, &t.xkc3, &t.zirows, &t.zirows3) == 10)
+    while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d %d %d %d", &k.nx, &k.ny, &k.nz, &k.mixed, &t.zrows,
+                       &t.yxt, &t.xkc, &t.xkc3, &t.zirows, &t.zirows3, &t.sx, &t.sy, &t.sz) == 13)
         g_tile_cache[k] = t;
     std::fclose(f);
 }
@@ -916,8 +959,8 @@ void append_tile_file(const TileKey &k, const Tiles &t)
     if (!path || !path[0]) return;
     FILE *f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d\n", k.nx, k.ny, k.nz, k.mixed, t.zrows, t.yxt, t.xkc, t.xkc3,
-                 t.zirows, t.zirows3);
+    std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d %d %d %d\n", k.nx, k.ny, k.nz, k.mixed, t.zrows, t.yxt, t.xkc,
+                 t.xkc3, t.zirows, t.zirows3, t.sx, t.sy, t.sz);
     std::fclose(f);
 }
 
@@ -942,6 +985,39 @@ int autotune_tiles(voce_rve *r)
     cudaEventCreate(&e1);
     Tiles best = r->tiles;
     int rc = VOCE_OK;
+    // one phase with tiles t: best of two rounds of 10 launches, after one
+    // warm-up launch (ms < 0: a CUDA error, recorded in rc)
+    auto time_phase = [&](const Tiles &t, int ph) -> float {
+        RveDesc dt = d;
+        dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc; dt.zirows = t.zirows;
+        dt.plx = schedule_of(d.nx, t.sx);
+        dt.ply = schedule_of(d.ny, t.sy);
+        dt.plz = schedule_of(d.nz, t.sz);
+        std::vector<RveDesc> one(1, dt);
+        RveDesc *pd = nullptr;
+        int2 *pm = nullptr;
+        BatchPlan bp;
+        rc = make_plan(one, r->precision, pd, pm, bp);
+        if (rc) return -1.f;
+        float ms = 1e30f;
+        cudaError_t e = launch_plan_phase(bp, ph, r->stream);
+        for (int round = 0; round < 2 && e == cudaSuccess; ++round) {
+            float t = 0.f;
+            e = cudaEventRecord(e0, r->stream);
+            for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = launch_plan_phase(bp, ph, r->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, r->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+            if (e == cudaSuccess && t < ms) ms = t;
+        }
+        cudaFree(pd);
+        cudaFree(pm);
+        if (e != cudaSuccess) {
+            rc = fail(VOCE_ERR_CUDA, "tile tuning: %s", cudaGetErrorString(e));
+            return -1.f;
+        }
+        return ms;
+    };
     const int phases[4] = {BP_ZF, BP_Y6, BP_XG, BP_ZI};
     for (int ph : phases) {
         int cand[8];
@@ -956,32 +1032,8 @@ int autotune_tiles(voce_rve *r)
             case BP_XG: t.xkc = cand[c]; break;
             default: t.zirows = cand[c]; break;
             }
-            RveDesc dt = d;
-            dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc; dt.zirows = t.zirows;
-            std::vector<RveDesc> one(1, dt);
-            RveDesc *pd = nullptr;
-            int2 *pm = nullptr;
-            BatchPlan bp;
-            rc = make_plan(one, r->precision, pd, pm, bp);
+            const float ms = time_phase(t, ph);
             if (rc) break;
-            // best of two rounds of 10 launches, after one warm-up launch
-            float ms = 1e30f;
-            cudaError_t e = launch_plan_phase(bp, ph, r->stream);
-            for (int round = 0; round < 2 && e == cudaSuccess; ++round) {
-                float t = 0.f;
-                e = cudaEventRecord(e0, r->stream);
-                for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = launch_plan_phase(bp, ph, r->stream);
-                if (e == cudaSuccess) e = cudaEventRecord(e1, r->stream);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-                if (e == cudaSuccess && t < ms) ms = t;
-            }
-            cudaFree(pd);
-            cudaFree(pm);
-            if (e != cudaSuccess) {
-                rc = fail(VOCE_ERR_CUDA, "tile tuning: %s", cudaGetErrorString(e));
-                break;
-            }
             if (ms < best_ms) {
                 best_ms = ms;
                 best_t = cand[c];
@@ -996,6 +1048,29 @@ int autotune_tiles(voce_rve *r)
             default: best.zirows = best_t; break;
             }
         }
+        // the radix schedule of the axis this phase transforms (z with the
+        // forward z pass, which the inverse one shares), with the chosen tile
+        if (ph == BP_ZI) continue;
+        const int L = ph == BP_ZF ? d.nz : ph == BP_Y6 ? d.ny : d.nx;
+        FftPlan1 sc[4];
+        const int ns = fft_schedules(L, sc, 4);
+        int &slot = ph == BP_ZF ? best.sz : ph == BP_Y6 ? best.sy : best.sx;
+        const int start = slot;
+        float sched_ms = best_ms;
+        for (int k = 0; k < ns && rc == VOCE_OK && ns > 1; ++k) {
+            if (k == start) continue;
+            Tiles t = best;
+            (ph == BP_ZF ? t.sz : ph == BP_Y6 ? t.sy : t.sx) = k;
+            const float ms = time_phase(t, ph);
+            if (rc) break;
+            // another schedule must be clearly faster: the default's order
+            // stays unless timing says otherwise
+            if (ms < 0.97f * sched_ms) {
+                sched_ms = ms;
+                slot = k;
+            }
+        }
+        if (rc) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1589,6 +1664,36 @@ int voce_rve_get_tiles(const voce_rve *r, int tiles[6])
     return VOCE_OK;
 }
 
+int voce_fft_schedule_count(int L)
+{
+    FftPlan1 c[4];
+    return fft_schedules(L, c, 4);
+}
+
+int voce_rve_get_fft_schedule(const voce_rve *r, int axis, int *radices, int max)
+{
+    if (!r || axis < 0 || axis > 2) return -fail(VOCE_ERR_ARG, "bad argument");
+    const FftPlan1 &p = axis == 0 ? r->d.plx : axis == 1 ? r->d.ply : r->d.plz;
+    for (int k = 0; k < p.nst && k < max && radices; ++k) radices[k] = p.rad[k];
+    return p.nst;
+}
+
+int voce_rve_set_fft_schedule(voce_rve *r, int axis, int k)
+{
+    if (!r || axis < 0 || axis > 2) return fail(VOCE_ERR_ARG, "bad argument");
+    if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch");
+    const int L = axis == 0 ? r->d.nx : axis == 1 ? r->d.ny : r->d.nz;
+    const int n = voce_fft_schedule_count(L);
+    if (k < 0 || k >= n) return fail(VOCE_ERR_ARG, "schedule %d of %d for length %d", k, n, L);
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    Tiles t = r->tiles;
+    (axis == 0 ? t.sx : axis == 1 ? t.sy : t.sz) = k;
+    apply_tiles(r, t);
+    if (r->graph_exec) { cudaGraphExecDestroy(r->graph_exec); r->graph_exec = nullptr; }
+    if (r->graph) { cudaGraphDestroy(r->graph); r->graph = nullptr; }
+    return VOCE_OK;
+}
+
 int voce_rve_set_tiles(voce_rve *r, const int tiles[6])
 {
     if (!r || !tiles) return fail(VOCE_ERR_ARG, "null argument");
@@ -1598,7 +1703,7 @@ int voce_rve_set_tiles(voce_rve *r, const int tiles[6])
     const int dim[6] = {d.ny, d.nx, d.ny, d.ny, d.ny, d.ny};
     for (int k = 0; k < 6; ++k)
         if (tiles[k] < 1 || dim[k] % tiles[k] != 0) return fail(VOCE_ERR_ARG, "tile %d = %d", k, tiles[k]);
-    Tiles t;
+    Tiles t = r->tiles;   // the radix schedules stay
     t.zrows = tiles[0]; t.yxt = tiles[1]; t.xkc = tiles[2];
     t.zirows = tiles[3]; t.xkc3 = tiles[4]; t.zirows3 = tiles[5];
     RveDesc dt = d;

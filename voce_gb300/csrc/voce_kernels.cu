@@ -906,12 +906,11 @@ __device__ double svm_of(const double *t9)
 
 // one thread: errors, volume averages, mixed-BC macro correction,
 // convergence decision (evolution.c:401-431, get_smacro :170-241)
-__device__ void finalize_iter_body(const RveDesc &d, int npart)
+__device__ void finalize_iter_body(const RveDesc &d, MacroDev *m, int npart)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
     if (threadIdx.x != 0) return;
-    MacroDev *m = d.macro;
     static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
     // the macro inputs, loaded together; the updates are computed in
     // registers and stored once (same operations, same order)
@@ -1251,12 +1250,11 @@ __device__ void prelude_unit(const RveDesc &d, int unit, int nunits)
 }
 
 
-__device__ void finalize_incr_body(const RveDesc &d, int npart)
+__device__ void finalize_incr_body(const RveDesc &d, MacroDev *m, int npart)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
     if (threadIdx.x != 0) return;
-    MacroDev *m = d.macro;
     double e6[6] = {tot[0], tot[1], tot[2], tot[3], tot[4], 0.0};
     double d6[6] = {tot[6], tot[7], tot[8], tot[9], tot[10], 0.0};
     double e9[9], d9[9];
@@ -1499,15 +1497,33 @@ __global__ void __launch_bounds__(128) kb_prelude(const RveDesc *descs, const in
 // one block per RVE.  With use_cond (a plan of one RVE), the iteration
 // finaliser also sets the condition of the graph's WHILE node: continue
 // while the RVE has not converged (evolution.c:342).
+// The RVE's descriptor and macro state are first copied into shared memory
+// by the whole block, so that the finaliser's single thread reads and
+// updates them at shared-memory latency instead of in a chain of dependent
+// global round trips; the macro state is written back once at the end.  The
+// arithmetic is unchanged.
 __global__ void __launch_bounds__(256) kb_finalize(const RveDesc *descs, int nrve, int incr_end,
                                                    cudaGraphConditionalHandle cond, int use_cond)
 {
+    static_assert(sizeof(RveDesc) % 8 == 0 && sizeof(MacroDev) % 8 == 0, "staged as 8-byte words");
+    constexpr int kDescWords = (int)(sizeof(RveDesc) / 8), kMacroWords = (int)(sizeof(MacroDev) / 8);
+    __shared__ unsigned long long s_desc[kDescWords];
+    __shared__ unsigned long long s_macro[kMacroWords];
     for (int r = blockIdx.x; r < nrve; r += gridDim.x) {
-        const RveDesc &d = descs[r];
-        if (!unit_on(d, incr_end ? MASK_CONVERGED : MASK_ACTIVE)) continue;
-        if (incr_end) finalize_incr_body(d, d.npart);
-        else finalize_iter_body(d, d.npart);
-        if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(cond, d.macro->converged ? 0u : 1u);
+        const RveDesc &dg = descs[r];
+        if (!unit_on(dg, incr_end ? MASK_CONVERGED : MASK_ACTIVE)) continue;
+        unsigned long long *gm = reinterpret_cast<unsigned long long *>(dg.macro);
+        const unsigned long long *gd = reinterpret_cast<const unsigned long long *>(&dg);
+        for (int i = threadIdx.x; i < kDescWords; i += blockDim.x) s_desc[i] = gd[i];
+        for (int i = threadIdx.x; i < kMacroWords; i += blockDim.x) s_macro[i] = gm[i];
+        __syncthreads();
+        const RveDesc &d = *reinterpret_cast<const RveDesc *>(s_desc);
+        MacroDev *m = reinterpret_cast<MacroDev *>(s_macro);
+        if (incr_end) finalize_incr_body(d, m, d.npart);
+        else finalize_iter_body(d, m, d.npart);
+        __syncthreads();
+        for (int i = threadIdx.x; i < kMacroWords; i += blockDim.x) gm[i] = s_macro[i];
+        if (use_cond && threadIdx.x == 0) cudaGraphSetConditional(cond, m->converged ? 0u : 1u);
         __syncthreads();
     }
 }

@@ -11,9 +11,11 @@ struct SetupConst {
     double sc6[6];            // B-basis Scauchy (creep start stress, init.c:523-525)
 };
 
-// FFT tile sizes (lines per block) for one grid
+// FFT tile sizes (lines per block) for one grid, and the radix schedule of
+// each axis (an index into fft_schedules' candidates of that axis' length)
 struct Tiles {
     int zrows, yxt, xkc, xkc3, zirows, zirows3;
+    int sx = 0, sy = 0, sz = 0;
     template <typename R> void choose(const RveDesc &d);
 };
 
