@@ -73,6 +73,10 @@ def parse():
     p.add_argument("--requests", type=int, default=32, help="cfg5: requests in the sample")
     p.add_argument("--rate", type=float, default=2.0, help="cfg5: Poisson arrival rate, req/s")
     p.add_argument("--budget-gb", type=float, default=200.0, help="cfg5: server HBM budget, GB")
+    p.add_argument("--active-voxels", type=int, default=4000000,
+                   help="cfg5: server active limit, voxels in flight (0: HBM budget alone)")
+    p.add_argument("--served-only", action="store_true",
+                   help="cfg5: serve the chosen form only (no other form, no plain FP64 server)")
     p.add_argument("--quantum", type=int, default=0,
                    help="cfg5: ticks after which a running request may be suspended (0: never)")
     p.add_argument("--inc-scale", type=float, default=0.1,
@@ -703,6 +707,7 @@ def run_cfg5(args):
             return lat, vi, span
         with capi.Server(precision, budget, ticks_per_round=16) as s:
             s.set_quantum(args.quantum)
+            s.set_active_limit(args.active_voxels)
             ids = []
             k = 0
             while True:
@@ -730,17 +735,18 @@ def run_cfg5(args):
 
     chosen = args.precision or "mixed_nr32"
     out = {}
-    for name, prec, single in (("served_" + chosen, PREC[chosen](), False),
-                               ("served_" + _other_mixed(chosen), PREC[_other_mixed(chosen)](), False),
-                               ("plain_fp64_one_at_a_time", capi.PREC_FP64, True)):
+    runs = (("served_" + chosen, PREC[chosen](), False),
+            ("served_" + _other_mixed(chosen), PREC[_other_mixed(chosen)](), False),
+            ("plain_fp64_one_at_a_time", capi.PREC_FP64, True))
+    for name, prec, single in runs[:1] if args.served_only else runs:
         lat, vi, span = serve(prec, single)
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "throughput": vi / span, "makespan_s": span, "voxel_iterations": vi}
         if not single:
             out[name]["preemptions"] = preempt[0]
-    b = out["plain_fp64_one_at_a_time"]
+    b = out.get("plain_fp64_one_at_a_time")
     for name, a in out.items():
-        if name != "plain_fp64_one_at_a_time":
+        if b is not None and name != "plain_fp64_one_at_a_time":
             a.update(throughput_ratio=a["throughput"] / b["throughput"],
                      p50_ratio=b["p50_s"] / a["p50_s"], p99_ratio=b["p99_s"] / a["p99_s"])
     a = out["served_" + chosen]
@@ -753,10 +759,11 @@ def run_cfg5(args):
                                "grains log-U[8,2048], random traceless loads, increments "
                                "round(%.2f x U{10..80}) (config 5 sample), continuous batching, "
                                "%s form" % (len(reqs), args.rate, args.inc_scale, chosen),
-                   "hbm_budget_gb": args.budget_gb, "quantum_ticks": args.quantum},
+                   "hbm_budget_gb": args.budget_gb, "quantum_ticks": args.quantum,
+                   "active_limit_voxels": args.active_voxels},
         "served": out,
-        "throughput_ratio": a["throughput_ratio"], "p50_ratio": a["p50_ratio"],
-        "p99_ratio": a["p99_ratio"],
+        "throughput_ratio": a.get("throughput_ratio"), "p50_ratio": a.get("p50_ratio"),
+        "p99_ratio": a.get("p99_ratio"),
     }
     print(json.dumps(res), flush=True)
 

@@ -54,6 +54,14 @@ int voce_server_submit(voce_server *s, const voce_namelist *nl,
  * resumes exactly where it stopped (bit-identical results).  0 (the
  * default): no suspension, first in first out. */
 int voce_server_set_quantum(voce_server *s, int ticks);
+/* Active limit: admit the queue head only while the voxels of the admitted
+ * requests, with it, stay at or under `voxels` (a request is always admitted
+ * when nothing runs).  Once the batch holds enough voxels to keep the GPU
+ * busy, more requests in flight only share it: each tick takes longer and
+ * every request finishes later.  A limit near that point keeps throughput
+ * and lets requests finish in arrival order, which lowers p50 and p99
+ * latency.  0 (the default): admission by HBM footprint alone. */
+int voce_server_set_active_limit(voce_server *s, long long voxels);
 /* One round; *running and *queued receive the counts afterwards. */
 int voce_server_poll(voce_server *s, int *running, int *queued);
 double voce_server_now(const voce_server *s);

@@ -100,3 +100,40 @@ def test_time_slicing_suspends_and_resumes_bit_for_bit(voce_lib):
             assert np.array_equal(s.result(rid, "sig_voigt", c.mesh.nvox), sig)
             pre += info.preemptions
         assert pre > 0
+
+
+def test_active_limit_keeps_voxels_in_flight_under_it(voce_lib):
+    """An active limit of 2 x 16^3 voxels: never more admitted than that (one
+    request always runs), requests still finish first in first out by
+    admission, and every result equals the request solved alone."""
+    rng = np.random.Generator(np.random.PCG64(79))
+    cases = []
+    for i, n in enumerate([16, 8, 16, 12, 16]):
+        c = synth.small_case(n, 6, 700 + i, n_steps=1, load=synth.random_traceless_load(rng))
+        c.iter_max = 30
+        cases.append(c)
+    alone = []
+    for c in cases:
+        nlp, _, _ = _inputs(c)
+        with capi.Rve.from_files(nlp) as r:
+            r.run(1)
+            alone.append(r.field("sig_voigt"))
+    limit = 2 * 16 ** 3
+    with capi.Server(capi.PREC_FP64, 64 << 30, ticks_per_round=3, keep_fields=True) as s:
+        s.set_active_limit(limit)
+        ids = []
+        for c in cases:
+            _, nl, sx = _inputs(c)
+            ids.append(s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, 1))
+        for _ in range(100000):
+            run, que = s.poll()
+            infos = [s.info(i) for i in ids]
+            active = sum(int(np.prod(x.dims)) for x in infos if x.status == capi.REQ_RUNNING)
+            assert active <= limit
+            if run == 0 and que == 0:
+                break
+        admits = [s.info(i).t_admit for i in ids]
+        assert admits == sorted(admits)
+        for rid, c, sig in zip(ids, cases, alone):
+            assert s.info(rid).status == capi.REQ_DONE
+            assert np.array_equal(s.result(rid, "sig_voigt", c.mesh.nvox), sig)

@@ -162,6 +162,7 @@ PROTOTYPES = [
     ("voce_rve_get_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]),
     ("voce_rve_set_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("voce_server_set_quantum", C.c_int, [C.c_void_p, C.c_int]),
+    ("voce_server_set_active_limit", C.c_int, [C.c_void_p, C.c_longlong]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -569,6 +570,11 @@ class Server:
 
     def set_quantum(self, ticks: int) -> None:
         _check(load().voce_server_set_quantum(self._h, ticks))
+
+    def set_active_limit(self, voxels: int) -> None:
+        """Admit only while the admitted requests hold at most this many
+        voxels (0: no limit)."""
+        _check(load().voce_server_set_active_limit(self._h, int(voxels)))
 
     def poll(self):
         run = C.c_int()

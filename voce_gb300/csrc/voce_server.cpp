@@ -35,6 +35,8 @@ struct voce_server {
     long long budget = 0, in_use = 0;
     int ticks_per_round = 1;
     int quantum = 0;                // ticks before a running request may be suspended
+    long long max_active = 0;       // voxels of the admitted requests at most (0: no limit)
+    long long active = 0;           // voxels of the admitted requests
     bool keep_fields = false;
     voce_batch *batch = nullptr;
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
@@ -49,6 +51,11 @@ struct voce_server {
 };
 
 namespace {
+
+long long voxels(const Request &q)
+{
+    return (long long)q.info.dims[0] * q.info.dims[1] * q.info.dims[2];
+}
 
 // Move a running request's state to host memory (a snapshot) and free its
 // device memory; it goes to the back of the queue and resumes, bit for bit,
@@ -66,6 +73,7 @@ int suspend(voce_server *s, Request &q)
     voce_rve_destroy(q.rve);
     q.rve = nullptr;
     s->in_use -= q.footprint;
+    s->active -= voxels(q);
     q.info.status = VOCE_REQ_QUEUED;
     q.info.preemptions += 1;
     q.ticks_run = 0;
@@ -101,6 +109,7 @@ void retire(voce_server *s, Request &q, int error)
         voce_rve_destroy(q.rve);
         q.rve = nullptr;
         s->in_use -= q.footprint;
+        s->active -= voxels(q);
     }
     q.info.status = error ? VOCE_REQ_FAILED : VOCE_REQ_DONE;
     q.info.error = error;
@@ -163,8 +172,10 @@ int voce_server_submit(voce_server *s, const voce_namelist *nl, const voce_slip 
 int voce_server_poll(voce_server *s, int *running, int *queued)
 {
     if (!s) return VOCE_ERR_ARG;
-    // admission: first in, first out, while the footprint fits; with a
-    // quantum, requests that have run that long make room by suspending
+    // admission: first in, first out, while the footprint fits (and the
+    // voxels in flight stay under the active limit, when one is set: a lone
+    // request is always admitted); with a quantum, requests that have run
+    // that long make room by suspending
     while (!s->queue.empty()) {
         Request &q = *s->reqs[s->queue.front()];
         if (q.footprint > s->budget) {
@@ -172,6 +183,7 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
             retire(s, q, VOCE_ERR_NOMEM);
             continue;
         }
+        if (s->max_active > 0 && !s->running.empty() && s->active + voxels(q) > s->max_active) break;
         if (s->in_use + q.footprint > s->budget) {
             Request *victim = nullptr;
             if (s->quantum > 0)
@@ -209,6 +221,7 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
             continue;
         }
         s->in_use += q.footprint;
+        s->active += voxels(q);
         q.info.status = VOCE_REQ_RUNNING;
         if (q.info.preemptions == 0) q.info.t_admit = s->now();
         q.ticks_run = 0;
@@ -242,6 +255,13 @@ int voce_server_set_quantum(voce_server *s, int ticks)
 {
     if (!s || ticks < 0) return VOCE_ERR_ARG;
     s->quantum = ticks;
+    return VOCE_OK;
+}
+
+int voce_server_set_active_limit(voce_server *s, long long voxels)
+{
+    if (!s || voxels < 0) return VOCE_ERR_ARG;
+    s->max_active = voxels;
     return VOCE_OK;
 }
 
