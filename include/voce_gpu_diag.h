@@ -84,6 +84,18 @@ int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
  * voce_rve_set_fft_schedule: use candidate k of axis; between calls,
  * outside a batch. */
 int voce_fft_schedule_count(int L);
+/* Chord steps in the FP64 Newton of the VOCE_PREC_MIXED form (no
+ * counterpart in the reference, which refreshes the Jacobian every Newton
+ * iteration, evolution.c:85-110): once a step has moved the stress by less
+ * than 1e-4 relative, the next one reuses its factored Jacobian.  The
+ * residual and the stop test are the reference's, and the converged stress
+ * moves by ~1e-14; but a chord step can add a Newton iteration, and the
+ * reference evaluates the strain rate and the error norms at the stress
+ * before the last update, so those move by up to ~1e-8 relative.  That is
+ * far inside the mixed form's error (single-precision spectrum) and outside
+ * the FP64 form's parity bound, so the FP64 form never takes chord steps.
+ * On (1) by default; applies to RVEs created afterwards. */
+int voce_set_newton_chord(int on);
 int voce_rve_get_fft_schedule(const voce_rve *r, int axis, int *radices, int max);
 int voce_rve_set_fft_schedule(voce_rve *r, int axis, int k);
 

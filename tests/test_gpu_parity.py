@@ -160,3 +160,23 @@ def test_gpu_rejects_bad_input(voce_lib):
     with pytest.raises(capi.VoceError) as e:
         capi.Rve.from_files(_write(synth.Case("r5", m, synth.CU_LIKE, synth.tension_z(), 0.2, 1)))
     assert e.value.code == 6
+
+
+def test_fp64_form_ignores_the_chord_switch(voce_lib):
+    """The FP64 form always refreshes the Jacobian (the reference's Newton
+    path): switching chord steps off changes none of its bits."""
+    make, n, _ = make_golden.CASES["vor12_mix"]
+    nl = _write(make())
+    lib = capi.load()
+    lib.voce_set_newton_chord(0)
+    try:
+        with capi.Rve.from_files(nl) as r:
+            r.run(2)
+            a = ([r.increment(k) for k in range(2)], r.field("sig_voigt"), r.field("edot_voigt"))
+    finally:
+        lib.voce_set_newton_chord(1)
+    with capi.Rve.from_files(nl) as r:
+        r.run(2)
+        b = ([r.increment(k) for k in range(2)], r.field("sig_voigt"), r.field("edot_voigt"))
+    assert a[0] == b[0]
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])

@@ -159,6 +159,7 @@ PROTOTYPES = [
     ("voce_rve_get_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_fft_schedule_count", C.c_int, [C.c_int]),
+    ("voce_set_newton_chord", C.c_int, [C.c_int]),
     ("voce_rve_get_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]),
     ("voce_rve_set_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("voce_server_set_quantum", C.c_int, [C.c_void_p, C.c_int]),

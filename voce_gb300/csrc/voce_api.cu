@@ -418,6 +418,7 @@ namespace {
 
 int autotune_tiles(voce_rve *r);
 extern int g_autotune;
+extern int g_newton_chord;
 
 // Device arrays of one RVE, state and scratch, sized from its descriptor;
 // the twiddle tables are filled, the rest is left to the caller.
@@ -571,6 +572,11 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     }
     d.plx = plx; d.ply = ply; d.plz = plz;
     d.mixed = r->precision != VOCE_PREC_FP64;
+    // chord steps only where the spectrum is single precision already: the
+    // FP64 form keeps the reference's Newton path, because the strain rate
+    // and the error norms are evaluated at the stress before the last Newton
+    // update (evolution.c:67,118-126), which moves with the step count
+    d.chord = r->precision == VOCE_PREC_MIXED ? g_newton_chord : 0;
     d.nr32 = r->precision == VOCE_PREC_MIXED_NR32;
     for (int p = 0; p < 2; ++p) d.solid[p + 1] = (p < nl->N_phases && !nl->Type_phases[p]) ? 1 : 0;
     d.nsys = sx.nsys;
@@ -702,6 +708,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     long long nph1 = 0;
     for (long long v = 0; v < nv; ++v) nph1 += mesh->phase[v] == 1;
     d.wgt_ph1 = (1.0 * (double)nph1) / Nxyz;
+    d.wgt_ratio = d.wgt / d.wgt_ph1;
 
     CUDA_TRY(launch_setup(d, sc, d_eul, r->npart, r->stream));
     std::vector<double> part((size_t)3 * r->npart * VOCE_NPART);
@@ -910,6 +917,7 @@ struct TileKey {
 std::mutex g_tile_mu;
 std::map<TileKey, Tiles> g_tile_cache;
 int g_autotune = 1;
+int g_newton_chord = 1;   // chord steps in the FP64 Newton of new VOCE_PREC_MIXED RVEs
 
 // schedule index k of an axis of length L (the default when out of range)
 FftPlan1 schedule_of(int L, int k)
@@ -1661,6 +1669,12 @@ int voce_rve_get_tiles(const voce_rve *r, int tiles[6])
     const Tiles &t = r->tiles;
     tiles[0] = t.zrows; tiles[1] = t.yxt; tiles[2] = t.xkc;
     tiles[3] = t.zirows; tiles[4] = t.xkc3; tiles[5] = t.zirows3;
+    return VOCE_OK;
+}
+
+int voce_set_newton_chord(int on)
+{
+    g_newton_chord = on ? 1 : 0;
     return VOCE_OK;
 }
 

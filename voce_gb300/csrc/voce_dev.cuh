@@ -85,8 +85,10 @@ struct RveDesc {
     int nsys, ipow_n;    // ipow_n >= 0: n integral, |r|^(n-1) by multiplication
     int update_flag, hard_flag, creep, iter_max;
     int mixed;           // spectrum precision: 0 double, 1 float
+    int chord;           // FP64 Newton: reuse the last Jacobian once the update is below 1e-4
     int nr32;            // Newton iterations in float with an FP64 acceptance step
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
+    double wgt_ratio;    // wgt / wgt_ph1 (the same IEEE division, once on the host)
     double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
     float gam0f[VOCE_NS], nrsf[VOCE_NS];   // float copies for the mixed Newton
     float gam0l[VOCE_NS];                  // gam0 - gam0f, rounded to float
@@ -518,9 +520,11 @@ __device__ __forceinline__ bool residual_ff(const RveDesc &d, long long v, const
 
 // Solve M x = b for symmetric positive definite M (6x6, full storage, only
 // the lower triangle read) by an LDL^T factorisation without pivoting.
-__device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)[6])
+// LDL^T factors of the symmetric 6x6 M (lower triangle read): L strictly
+// below the diagonal, dinv = 1/D
+__device__ __forceinline__ void ldlt_factor6(const double (&M)[6][6], double (&L)[6][6], double (&dinv)[6])
 {
-    double L[6][6], w[6][6], dinv[6];
+    double w[6][6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         double dj = M[j][j];
@@ -536,6 +540,11 @@ __device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)
             L[i][j] = s * dinv[j];
         }
     }
+}
+
+// b := M^-1 b from the factors of ldlt_factor6
+__device__ __forceinline__ void ldlt_apply6(const double (&L)[6][6], const double (&dinv)[6], double (&b)[6])
+{
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         double s = b[i];
@@ -552,6 +561,13 @@ __device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)
         for (int k = i + 1; k < 6; ++k) s = fma(-L[k][i], b[k], s);
         b[i] = s;
     }
+}
+
+__device__ __forceinline__ void ldlt_solve6(const double (&M)[6][6], double (&b)[6])
+{
+    double L[6][6], dinv[6];
+    ldlt_factor6(M, L, dinv);
+    ldlt_apply6(L, dinv, b);
 }
 
 // ---------------------------------------------------------------------------

@@ -42,36 +42,40 @@ __device__ void block_partials(double (&acc)[VOCE_NPART], double *out)
 }
 
 // sum the per-block partials of one kernel in a fixed order (one block of
-// 256 threads): 16 stripes per quantity, 8 independent loads in flight per
-// thread, then the stripes in order
+// 256 threads): thread t takes quantity t % 16 over stripe t / 16, a run of
+// consecutive blocks, with up to 32 loads in flight and a pairwise tree over
+// them; the 16 stripe sums are then added pairwise too.  Entry 15 is a max
+// (of non-negative counts, so 0 is its identity as for the sums).
 __device__ void reduce_partials(const double *part, int npart, double (&tot)[VOCE_NPART])
 {
     __shared__ double red[16][VOCE_NPART];
     const int t = threadIdx.x;  // blockDim.x == 256
     const int q = t % VOCE_NPART, stripe = t / VOCE_NPART;
     const bool mx = q == VOCE_NPART - 1;
-    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int b = stripe;
-    for (; b + 7 * 16 < npart; b += 8 * 16) {
-        double x[8];
+    const int chunk = (npart + 15) / 16;
+    const int b0 = stripe * chunk, b1 = min(npart, b0 + chunk);
+    double s = 0.0;
+    for (int b = b0; b < b1; b += 32) {
+        double x[32];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) x[k] = part[(long long)(b + 16 * k) * VOCE_NPART + q];
+        for (int k = 0; k < 32; ++k) x[k] = (b + k < b1) ? part[(long long)(b + k) * VOCE_NPART + q] : 0.0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = mx ? fmax(a[k], x[k]) : a[k] + x[k];
+        for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+            for (int k = 0; k < w; ++k) x[k] = mx ? fmax(x[k], x[k + w]) : x[k] + x[k + w];
+        s = mx ? fmax(s, x[0]) : s + x[0];
     }
-    for (int k = 0; b < npart; b += 16, ++k) {
-        const double x = part[(long long)b * VOCE_NPART + q];
-        a[k & 7] = mx ? fmax(a[k & 7], x) : a[k & 7] + x;
-    }
-    double s = a[0];
-#pragma unroll
-    for (int k = 1; k < 8; ++k) s = mx ? fmax(s, a[k]) : s + a[k];
     red[stripe][q] = s;
     __syncthreads();
     if (t < VOCE_NPART) {
-        double v = red[0][t];
-        for (int k = 1; k < 16; ++k) v = (t == VOCE_NPART - 1) ? fmax(v, red[k][t]) : v + red[k][t];
-        red[0][t] = v;
+        double v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = red[k][t];
+#pragma unroll
+        for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+            for (int k = 0; k < w; ++k) v[k] = mx ? fmax(v[k], v[k + w]) : v[k] + v[k + w];
+        red[0][t] = v[0];
     }
     __syncthreads();
 #pragma unroll
@@ -573,14 +577,27 @@ __device__ __forceinline__ void reload_P(const RveDesc &d, long long v, double (
 // Newton steps on the FP64 residual with the stop test of evolution.c:112.
 // NR32 (fallback of the single-precision form only): the Jacobian and its
 // solve in FP32, an inexact Newton step converging to the same FP64 fixed
-// point; otherwise all FP64.
-template <bool NR32>
+// point; otherwise all FP64.  With d.chord (the VOCE_PREC_MIXED form), an
+// FP64 step whose predecessor moved the stress by less than 1e-4 relative
+// reuses that predecessor's factored Jacobian (a chord step: the residual,
+// the flow rule's strain rate and the stop test are evaluated as always, the
+// Jacobian and its LDL^T factorisation are not).  Near the root the Jacobian
+// then differs by about n x 1e-4 relative, so each chord step still divides
+// the error by ~500; the converged stress moves by ~1e-14 relative against
+// the exact-Jacobian Newton of the reference (evolution.c:85-110), the point
+// before the last update (where the strain rate is evaluated) by up to 1e-8
+// when the step count changes.
+template <bool NR32, bool CHORD = false>
 __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const double (&P)[21],
                                            const double (&cc)[6], double thr, double (&sig)[6],
                                            double (&sp)[6], double (&Rl)[6], int &it)
 {
     const double dt = d.dt;
     bool go = true;
+    // FP64 Jacobian factors, kept for chord steps (CHORD instances only)
+    double L[6][6], dinv[6];
+    bool fresh = true;
+    (void)L; (void)dinv; (void)fresh;
     while (go && it < 100) {
         ++it;
         double ed[5];
@@ -612,7 +629,7 @@ __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const
             ldlt_solve6f(M, x);
 #pragma unroll
             for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
-        } else {
+        } else if (!CHORD) {
             double D[15];
             flow_rule<true, false, double>(d, v, sig, ed, D, nullptr, nullptr);
 #pragma unroll
@@ -633,6 +650,32 @@ __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const
                     M[i][j] = m;
                 }
             ldlt_solve6(M, R);
+        } else {
+            if (fresh) {
+                double D[15];
+                flow_rule<true, false, double>(d, v, sig, ed, D, nullptr, nullptr);
+                double M[6][6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+#pragma unroll
+                    for (int j = 0; j <= i; ++j) {
+                        double m = P[sym6(i, j)];
+                        if (i < 5 && j < 5) m = fma(dt, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                        M[i][j] = m;
+                    }
+                ldlt_factor6(M, L, dinv);
+            } else {
+                flow_rule<false, false, double>(d, v, sig, ed, (double *)nullptr, nullptr, nullptr);
+            }
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                double s = cc[i] + (i < 5 ? dt * ed[i] : 0.0);
+#pragma unroll
+                for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+                R[i] = s;
+                Rl[i] = s;
+            }
+            ldlt_apply6(L, dinv, R);
         }
         double cnr = 0.0;
 #pragma unroll
@@ -643,6 +686,9 @@ __device__ __forceinline__ void newton_fp64(const RveDesc &d, long long v, const
             sig[c] = sn;
         }
         go = cnr > thr;
+        // the next step reuses this Jacobian (a chord step) once the update
+        // is below 1e-4 relative (cnr <= 1e-8 sn2 = 1e6 thr)
+        if (CHORD) fresh = !d.chord || cnr > 1e6 * thr;
     }
 }
 
@@ -743,7 +789,7 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
     }
 }
 
-template <bool NR32>
+template <bool NR32, bool CHORD = false>
 __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 {
     // per-thread sums in shared memory (one slot per thread, the same
@@ -813,7 +859,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             double P[21];
             load_P(d, v, P);
             // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
-            newton_fp64<false>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            newton_fp64<false, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
         }
         double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
         if (NR32) {
@@ -932,7 +978,7 @@ __device__ void finalize_iter_body(const RveDesc &d, MacroDev *m, int npart)
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         sa[q] = s9[q] * d.wgt;
-        sa1[q] = s19[q] * (d.wgt / d.wgt_ph1);
+        sa1[q] = s19[q] * d.wgt_ratio;
         m->SigAvg[q] = sa[q];
         m->SigAvg1[q] = sa1[q];
     }
@@ -1462,7 +1508,9 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
 #define VOCE_NR_MIXED_BLOCKS 3
 #endif
 
-template <bool NR32>
+// CHORD: the FP64 Newton may take chord steps (VOCE_PREC_MIXED plans; each
+// RVE's d.chord decides); the FP64 form's instance is the exact-Jacobian one
+template <bool NR32, bool CHORD = false>
 __global__ void __launch_bounds__(128, NR32 ? VOCE_NR_MIXED_BLOCKS : 1)
 kb_nr(const RveDesc *descs, const int2 *map, int total)
 {
@@ -1470,7 +1518,7 @@ kb_nr(const RveDesc *descs, const int2 *map, int total)
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
         if (!unit_on(d, MASK_ACTIVE)) continue;
-        nr_unit<NR32>(d, e.y, d.npart);
+        nr_unit<NR32, CHORD>(d, e.y, d.npart);
     }
 }
 
@@ -1695,6 +1743,9 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     pf.begin(K_NR, s);
     if (bp.nr32)
         kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), VOCE_NR_THREADS, kNrStageBytes, s>>>(
+            D, bp.map[BP_NP], bp.total[BP_NP]);
+    else if (bp.mixed)
+        kb_nr<false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else
         kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), VOCE_NR_THREADS, 0, s>>>(
