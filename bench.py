@@ -212,8 +212,9 @@ KB_NR_FP64_FLOPS_PER_VOXEL = 307
 
 
 # The same for kb_nr<1> (mixed_nr32 form, profiles/kb_nr_nr32_cfg2_64.md); the
-# mixed form runs the FP64 form's Newton kernel.
-KB_NR_NR32_DRAM_BYTES = 387.5e6
+# mixed form's chord-step instance of the FP64 Newton kernel moves the same
+# bytes as the FP64 one (profiles/kb_nr_mixed_cfg2_64.md: 269.1 MB).
+KB_NR_NR32_DRAM_BYTES = 276.2e6
 
 
 def profiled_traffic(precision="fp64"):
