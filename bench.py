@@ -462,6 +462,14 @@ def run_cfg3(args):
         incs = [r.increment(k) for k in range(args.warmup + args.steps)]
         out[name] = {"value": nv * its / (ms * 1e-3), "ms": ms, "iters": its,
                      "incs": incs, "sig": r.field("sig_voigt"), "edot": r.field("edot_voigt")}
+        # where the time goes: one more increment, host-driven, every launch
+        # bracketed by CUDA events (same kernels; after the timed region)
+        r.set_profiling(True)
+        r.reset_kernel_times()
+        r.run(1)
+        n_it = r.increment(args.warmup + args.steps)["iters"]
+        out[name]["kernel_us_per_iteration"] = {
+            k: round(1e3 * t / n_it, 1) for k, (t, n) in r.kernel_times().items() if n > 0}
         r.close()
 
     def rel(x, y):
@@ -470,11 +478,13 @@ def run_cfg3(args):
         return float(np.abs(x - y).max() / np.abs(y).max())
 
     b = out["fp64"]
-    forms = {"fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"]}}
+    forms = {"fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"],
+                      "kernel_us_per_iteration": b["kernel_us_per_iteration"]}}
     for name in ("mixed", "mixed_nr32"):
         a = out[name]
         forms[name] = {
             "value": a["value"], "ms_per_step": a["ms"] / args.steps, "iters": a["iters"],
+            "kernel_us_per_iteration": a["kernel_us_per_iteration"],
             "over_fp64": a["value"] / b["value"], "arithmetic": FORM_DOC[name],
             "error_vs_fp64": {
                 "macro_stress_max_rel": max(rel(x["sig_avg"], y["sig_avg"])

@@ -777,10 +777,13 @@ __device__ typename Cx<R>::T *fft_lines(typename Cx<R>::T *a, typename Cx<R>::T 
         const int r = pl.rad[st];
         const int m = ncur / r;
         const int nb = NL * (L / r);
+        // butterfly bi = (p s + q) NL + l: the thread's first (l, q, p) and the
+        // step to its next one (bi + nthr) by two divisions per stage, then
+        // carried forward, instead of three divisions per butterfly
+        int l = tid % NL, q = tid / NL, p = q / s;
+        q -= p * s;
+        const int dl = nthr % NL, dt = nthr / NL, dp = dt / s, dq = dt - dp * s;
         for (int bi = tid; bi < nb; bi += nthr) {
-            const int l = bi % NL;
-            const int t = bi / NL;
-            const int p = t / s, q = t - (t / s) * s;
             C x[4], y[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j)
@@ -819,6 +822,13 @@ __device__ typename Cx<R>::T *fft_lines(typename Cx<R>::T *a, typename Cx<R>::T 
                 C z = (e == 0) ? y[k] : cmul<R>(y[k], w);
                 dst[(q + s * (r * p + k)) * ldl + l] = z;
             }
+            // (l, q, p) of bi + nthr
+            l += dl;
+            int c = 0;
+            if (l >= NL) { l -= NL; c = 1; }
+            q += dq + c;
+            p += dp;
+            if (q >= s) { q -= s; p += 1; }
         }
         __syncthreads();
         ncur = m;
