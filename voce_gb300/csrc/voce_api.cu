@@ -709,6 +709,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     for (long long v = 0; v < nv; ++v) nph1 += mesh->phase[v] == 1;
     d.wgt_ph1 = (1.0 * (double)nph1) / Nxyz;
     d.wgt_ratio = d.wgt / d.wgt_ph1;
+    d.all_ph1 = nph1 == nv ? 1 : 0;
 
     CUDA_TRY(launch_setup(d, sc, d_eul, r->npart, r->stream));
     std::vector<double> part((size_t)3 * r->npart * VOCE_NPART);

@@ -89,6 +89,7 @@ struct RveDesc {
     int nr32;            // Newton iterations in float with an FP64 acceptance step
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double wgt_ratio;    // wgt / wgt_ph1 (the same IEEE division, once on the host)
+    int all_ph1;         // every voxel is phase 1 (the phase-1 sums equal the full ones)
     double gam0[VOCE_NS], nrs[VOCE_NS], g0n[VOCE_NS];
     float gam0f[VOCE_NS], nrsf[VOCE_NS];   // float copies for the mixed Newton
     float gam0l[VOCE_NS];                  // gam0 - gam0f, rounded to float

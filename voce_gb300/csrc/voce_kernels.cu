@@ -796,6 +796,9 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     // additions in the same order as register accumulators) keep them out of
     // the registers the Newton loop needs
     __shared__ double s_acc[VOCE_NPART][VOCE_NR_THREADS];
+    // Newton iteration count (sum, max) as integers; entries 14 and 15 of
+    // the partials receive them converted, the same values
+    __shared__ int s_it[2][VOCE_NR_THREADS];
     const int tid = threadIdx.x;
     // NR32: this thread's column of the staged float model data
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -807,6 +810,8 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     }
 #pragma unroll
     for (int q = 0; q < VOCE_NPART; ++q) s_acc[q][tid] = 0.0;
+    s_it[0][tid] = 0;
+    s_it[1][tid] = 0;
     const long long nv = d.nv;
     for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
          v += (long long)nunits * blockDim.x) {
@@ -901,16 +906,24 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
         s_acc[1][tid] += nce;
 #pragma unroll
         for (int c = 0; c < 6; ++c) s_acc[2 + c][tid] += sig[c];
-        if (ph == 1) {
+        // phase-1 sums; when every voxel is phase 1 they would repeat the
+        // sums above addition for addition, and are copied from them below
+        if (ph == 1 && !d.all_ph1) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) s_acc[8 + c][tid] += sig[c];
         }
-        s_acc[14][tid] += (double)it;
-        s_acc[15][tid] = fmax(s_acc[15][tid], (double)it);
+        s_it[0][tid] += it;
+        s_it[1][tid] = max(s_it[1][tid], it);
     }
     double acc[VOCE_NPART];
 #pragma unroll
     for (int q = 0; q < VOCE_NPART; ++q) acc[q] = s_acc[q][tid];
+    if (d.all_ph1) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[8 + c] = acc[2 + c];
+    }
+    acc[14] = (double)s_it[0][tid];
+    acc[15] = (double)s_it[1][tid];
     block_partials(acc, d.part + (long long)unit * VOCE_NPART);
 }
 
