@@ -165,17 +165,20 @@ __host__ __device__ __forceinline__ int sym6(int i, int j)
     return a * 6 - (a * (a - 1)) / 2 + (b - a);
 }
 
-// Newton-Raphson reciprocal: a single-precision seed refined by two steps
-// of r <- r + r(1 - x r), each of which squares the relative error
-// (2^-23 -> 2^-46 -> below 2^-52 up to rounding); outside the range where
-// the float seed is meaningful it falls back to division.  It is used only
-// inside the 6x6 solve of the Newton step, whose accuracy shapes the step
-// and not the converged stress.
+// Newton-Raphson reciprocal: the hardware's approximate double reciprocal
+// (rcp.approx.ftz.f64, about 20 correct bits) refined by two steps of
+// r <- r + r(1 - x r), each of which squares the relative error (down to
+// rounding); outside 2^-99 <= |x| < 2^99 it falls back to division.  The
+// range test reads the exponent bits with integer operations, and the seed
+// needs no conversions, which keeps both off the FP64 pipe.  It is used
+// inside the 6x6 solve of the Newton step and for the Green operator's 3x3
+// inverse.
 __device__ __forceinline__ double rcp_nr(double x)
 {
-    double ax = fabs(x);
-    if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
-    double r = (double)(1.0f / (float)x);
+    const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    if (hi - 0x39C00000u >= 0x46200000u - 0x39C00000u) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
     double e = fma(-x, r, 1.0);
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
@@ -263,7 +266,10 @@ __device__ __forceinline__ void flow_rule(const RveDesc &d, long long v, const d
 #pragma unroll
         for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
         const double rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
-        const int neg = rss < 0.0;
+        // the sign bit by an integer test (for rss = -0 it picks the backward
+        // CRSS, where a float compare picks the forward one; both give zero
+        // shear rate and a zero tangent term)
+        const int neg = __double2hiint(rss) < 0;
         const double it = __ldg(d.itau + (long long)(2 * k + neg) * nv + v);
         const double r = rss * it;
         double g1, g2;
