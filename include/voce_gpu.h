@@ -62,8 +62,18 @@ enum {
  *                         FP32 ended by an acceptance step on the FP64
  *                         residual (relative update below 1e-5), FP32-only
  *                         while the Green error is above 1e-4; per-voxel error
- *                         norms in FP32 (their sums in FP64). */
-enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1, VOCE_PREC_MIXED_NR32 = 2 };
+ *                         norms in FP32 (their sums in FP64).  The Newton
+ *                         iterations and the norms are not FP64 here.
+ *   VOCE_PREC_MIXED_IR    spectrum and Green-operator convolution in FP32;
+ *                         every Newton iteration evaluates the residual and
+ *                         the flow rule (resolved shears, power law, strain
+ *                         rate) in FP64 and takes its stop test in FP64, and
+ *                         only the correction -- the Jacobian's assembly and
+ *                         its LDL^T solve -- is FP32 (iterative refinement:
+ *                         the converged stress is the root of the FP64
+ *                         residual); hardening, averages and the per-voxel
+ *                         error norms in FP64. */
+enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1, VOCE_PREC_MIXED_NR32 = 2, VOCE_PREC_MIXED_IR = 3 };
 
 /* Every variable the reference's namelist reader knows (io.c:25-52), with
  * the reference's names, types and lengths. */

@@ -52,6 +52,13 @@ void *voce_host_alloc(long long bytes);
 void voce_host_free(void *p);
 /* FP64 FMA throughput of the current device, TFLOP/s (FMA = 2 flops). */
 double voce_measure_fp64_tflops(void);
+/* Free and total memory of the current device, bytes (cudaMemGetInfo). */
+int voce_device_memory(long long *free_bytes, long long *total_bytes);
+/* out[i] = the reciprocal the FP64 Newton step and the Green operator use
+ * (a hardware seed refined by two Newton-Raphson steps, plain division
+ * outside 2^-99 <= |x| < 2^99), computed on the current device for n host
+ * values: a check of that reciprocal against 1/x. */
+int voce_diag_rcp(const double *x, double *out, int n);
 
 /* FFT tile tuning.  voce_rve_create times the forward-pass FFT phases with
  * a few tile sizes (lines per block) on the new RVE and keeps the fastest,
@@ -72,12 +79,18 @@ int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
  * transforms to FFTW).  Each axis of length L = 2^a 3^b runs as Stockham
  * passes of radix 4, 2 and 3; the candidate schedules are their stage orders
  * 4s-2-3s (the default), 3s-4s-2, 2-4s-3s and 3s-2-4s, duplicates dropped.
- * With tuning on, voce_rve_create times the candidates of each axis on the
- * forward pass that transforms it (with the tuned tile) and keeps one only
- * when it is more than 3 % faster than the default; the choice is cached
- * with the tiles (and in VOCE_TILE_CACHE).  Unlike the tiles, the schedule
- * changes results in the last bits (a different order of roundings); an RVE
- * keeps its schedule for life, in a batch and through snapshots.
+ * Unlike the tiles, the schedule changes results in the last bits (a
+ * different order of roundings).  So the FP64 form never tunes it: its RVEs
+ * run the default schedule of every axis unless the caller sets one, and its
+ * results are the same bits in every process.  For the single-precision
+ * spectrum forms (VOCE_PREC_MIXED, VOCE_PREC_MIXED_NR32), with tuning on,
+ * voce_rve_create times the candidates of each axis on the forward pass that
+ * transforms it (with the tuned tile) and keeps one only when it is more than
+ * 3 % faster than the default; the choice is cached with the tiles (and in
+ * VOCE_TILE_CACHE).  Their bits can therefore differ between processes whose
+ * tuning timed differently (within the form's single-precision error), but
+ * not within a process: an RVE keeps its schedule for life, alone, in a
+ * batch, in the server and through snapshots.
  * voce_fft_schedule_count: candidates for length L (0 if not 2^a 3^b).
  * voce_rve_get_fft_schedule: the radices of axis (0 x, 1 y, 2 z) in stage
  * order; returns the number of stages (at most max written), < 0 on error.

@@ -19,7 +19,18 @@ PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 PORT_BIN = os.path.join(HERE, "_build", "evp_oracle")
 REF_BIN = os.path.join(HERE, "_ref", "evp_ref")
 REF_LIB = os.path.join(HERE, "_ref", "libevp_ref.so")
-REFERENCE_SRC = "/root/reference"
+# where the reference sources lie: given by the caller, by the environment
+# variable VOCE_REFERENCE_SRC, or else a directory "reference" beside the
+# repository's own directory
+REFERENCE_ENV = "VOCE_REFERENCE_SRC"
+
+
+def reference_src() -> str:
+    """The reference source directory, or "" when there is none."""
+    src = os.environ.get(REFERENCE_ENV, "")
+    if not src:
+        src = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return os.path.abspath(src) if os.path.isfile(os.path.join(src, "evolution.c")) else ""
 
 FIELDS = {"sig": (0, 9), "eps": (1, 9), "edot": (2, 9), "disgrad": (3, 9),
           "tranmat": (4, 9), "crss": (5, 12), "gamdot": (6, 12), "gamacum": (7, 1),
@@ -31,11 +42,13 @@ def build_port() -> str:
     return PORT_LIB
 
 
-def build_ref() -> bool:
-    """Compile the reference sources with the shims, when they are present."""
-    if not os.path.isdir(REFERENCE_SRC):
+def build_ref(src: str | None = None) -> bool:
+    """Compile the reference sources in directory ``src`` (default:
+    reference_src()) with the shims; False when there are none."""
+    src = src or reference_src()
+    if not src or not os.path.isdir(src):
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_SRC], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + os.path.abspath(src)], check=True)
     return True
 
 

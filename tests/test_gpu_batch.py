@@ -42,7 +42,7 @@ def _same(a, b):
         assert np.array_equal(u, v)
 
 
-@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32])
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32, capi.PREC_MIXED_IR])
 def test_alone_equals_in_batch(prec, voce_lib):
     cases = _cases()
     alone = []

@@ -1,8 +1,10 @@
 """The mixed-precision forms against the reference's own macro curve and
 fields (golden fixtures) and against the FP64 form on the GPU:
 VOCE_PREC_MIXED (FP32 spectrum and Green operator, FP64 Newton, hardening,
-norms and averages) and VOCE_PREC_MIXED_NR32 (the same with FP32 Newton
-iterations ended by an FP64-residual acceptance step).
+norms and averages), VOCE_PREC_MIXED_IR (the same with the Newton correction
+-- Jacobian and LDL^T solve -- in FP32, the residual, flow rule, stop test and
+norms in FP64) and VOCE_PREC_MIXED_NR32 (FP32 Newton iterations ended by an
+FP64-residual acceptance step).
 
 Bounds: the macro stress / strain / strain-rate averages of every increment
 within 1e-4 relative (the bound the mixed form is held to); per-voxel stress
@@ -29,7 +31,7 @@ def _write(case):
     return case.write(tempfile.mkdtemp(prefix="mixed_"))
 
 
-FORMS = [capi.PREC_MIXED, capi.PREC_MIXED_NR32]
+FORMS = [capi.PREC_MIXED, capi.PREC_MIXED_IR, capi.PREC_MIXED_NR32]
 
 
 @pytest.mark.parametrize("prec", FORMS)
@@ -115,3 +117,31 @@ def test_mixed_chord_steps_against_exact_jacobian(name, voce_lib):
         assert gio.rel(np.array(a["sig_avg"]) * nv, ref["its"][-1]["sig"].ravel()) < MACRO_TOL
     assert gio.rel(chord[1], exact[1]) < 1e-6
     assert gio.rel(chord[2], exact[2]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["vor8_psc", "vor12_mix", "cfg1_16"])
+def test_float_jacobian_converges_to_the_fp64_residual_root(name, voce_lib):
+    """VOCE_PREC_MIXED_IR against VOCE_PREC_MIXED with the exact FP64
+    Jacobian (chord steps off): both drive the same FP64 residual to its root
+    under the same stop test, so they differ only by where each stops
+    (updates below 1e-7 relative) -- macro averages within 1e-7, fields
+    within 1e-6, Green-iteration counts within one."""
+    make, n, _ = make_golden.CASES[name]
+    case = make()
+    nl = _write(case)
+    lib = capi.load()
+    lib.voce_set_newton_chord(0)
+    try:
+        with capi.Rve.from_files(nl, capi.PREC_MIXED) as r:
+            r.run(n)
+            exact = ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"))
+    finally:
+        lib.voce_set_newton_chord(1)
+    with capi.Rve.from_files(nl, capi.PREC_MIXED_IR) as r:
+        r.run(n)
+        ir = ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"))
+    for a, b in zip(ir[0], exact[0]):
+        assert abs(a["iters"] - b["iters"]) <= 1
+        assert gio.rel(a["sig_avg"], b["sig_avg"]) < 1e-7
+    assert gio.rel(ir[1], exact[1]) < 1e-6
+    assert gio.rel(ir[2], exact[2]) < 1e-6

@@ -31,7 +31,7 @@ def _same(a, b):
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32])
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED, capi.PREC_MIXED_NR32, capi.PREC_MIXED_IR])
 def test_restore_continues_bit_for_bit(prec, voce_lib):
     nl = _case(71)
     with capi.Rve.from_files(nl, prec) as r:

@@ -60,10 +60,11 @@ def test_test_host_links(legacy_lib):
 
 def test_reference_program_links_against_legacy_library(legacy_lib):
     import oracle
-    if not os.path.isdir(oracle.REFERENCE_SRC):
+    src = oracle.reference_src()
+    if not src:
         pytest.skip("reference sources not present")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "legacy-link",
-                    "REF=" + oracle.REFERENCE_SRC], check=True)
+                    "REF=" + src], check=True)
     for exe in ("evp_gpu_cxx", "evp_gpu_c"):
         assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", exe))
 

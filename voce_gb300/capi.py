@@ -21,7 +21,7 @@ VOCE_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
           5: "ERR_SINGULAR", 6: "ERR_UNSUPPORTED", 7: "ERR_NOMEM", 8: "ERR_CUDA",
           9: "ERR_STATE"}
-PREC_FP64, PREC_MIXED, PREC_MIXED_NR32 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_MIXED_NR32, PREC_MIXED_IR = 0, 1, 2, 3
 NOALLOC_MAX_DOUBLES = 4194304   # VOCE_NOALLOC_MAX_DOUBLES
 # .iout dump kinds (include/voce_io.h)
 IOUT = {"eps": 0, "sig": 1, "els": 2, "edot": 3, "slip": 4, "taux": 5, "crss": 6, "tex": 7,
@@ -125,6 +125,8 @@ PROTOTYPES = [
     ("voce_host_alloc", C.c_void_p, [C.c_longlong]),
     ("voce_host_free", None, [C.c_void_p]),
     ("voce_measure_fp64_tflops", C.c_double, []),
+    ("voce_device_memory", C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    ("voce_diag_rcp", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
     # voce_batch.h
     ("voce_batch_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     ("voce_batch_add", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
@@ -245,6 +247,21 @@ def read_mesh(path: str, dims: Sequence[int]):
 
 def footprint(dims: Sequence[int], precision: int = PREC_FP64) -> int:
     return int(load().voce_rve_footprint((C.c_int * 3)(*dims), precision))
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    f, t = C.c_longlong(), C.c_longlong()
+    _check(load().voce_device_memory(C.byref(f), C.byref(t)))
+    return int(f.value), int(t.value)
+
+
+def diag_rcp(x: np.ndarray) -> np.ndarray:
+    """The library's device reciprocal (voce_diag_rcp) of every value of x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    _check(load().voce_diag_rcp(_dptr(x), _dptr(out), x.size))
+    return out
 
 
 class Rve:

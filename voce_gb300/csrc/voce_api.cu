@@ -436,8 +436,10 @@ int alloc_device(voce_rve *r)
     d.itau32 = nullptr;
     d.sgp32 = nullptr;
     d.sch_lo = d.itau_lo = d.sgp_lo = nullptr;
-    if (d.nr32) {
+    if (d.nr32 || d.ir) {
         AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv);
+    }
+    if (d.nr32) {
         AL(d.sch_lo, 60 * nv); AL(d.itau_lo, 24 * nv); AL(d.sgp_lo, 21 * nv);
     }
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
@@ -485,10 +487,12 @@ void for_state(RveDesc &d, F &&f)
     f((void **)&d.taux, 12 * nv * D);    f((void **)&d.svm, nv * D);
     f((void **)&d.evm, nv * D);          f((void **)&d.rotl, 3 * nv * D);
     f((void **)&d.diag, 3 * nv * D);     f((void **)&d.phase, nv * sizeof(int));
-    if (d.nr32) {
+    if (d.nr32 || d.ir) {
         f((void **)&d.sch32, 60 * nv * S);
         f((void **)&d.itau32, 24 * nv * S);
         f((void **)&d.sgp32, 21 * nv * S);
+    }
+    if (d.nr32) {
         f((void **)&d.sch_lo, 60 * nv * S);
         f((void **)&d.itau_lo, 24 * nv * S);
         f((void **)&d.sgp_lo, 21 * nv * S);
@@ -512,8 +516,10 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
     // + the FP64 form's stored Green-operator frequencies, 9 doubles each
-    // + the mixed_nr32 form's float pairs of sch, itau and S_g + S0 (2 x 105 floats)
-    return nv * (214 * 8 + 4 + (precision == VOCE_PREC_MIXED_NR32 ? 840 : 0)) + nspec * 9 * cplx +
+    // + the mixed_nr32 form's float pairs of sch, itau and S_g + S0 (2 x 105
+    // floats), the mixed_ir form's float copies of the same (105 floats)
+    const long long f32 = precision == VOCE_PREC_MIXED_NR32 ? 840 : precision == VOCE_PREC_MIXED_IR ? 420 : 0;
+    return nv * (214 * 8 + 4 + f32) + nspec * 9 * cplx +
            (precision == VOCE_PREC_FP64 ? nspec * 9 * 8 : 0);
 }
 
@@ -555,7 +561,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
             return fail(VOCE_ERR_PARSE, "phase id %d at voxel %lld", mesh->phase[v], v);
 
     voce_rve *r = new voce_rve();
-    if (precision != VOCE_PREC_FP64 && precision != VOCE_PREC_MIXED && precision != VOCE_PREC_MIXED_NR32) {
+    if (precision < VOCE_PREC_FP64 || precision > VOCE_PREC_MIXED_IR) {
         delete r;
         return fail(VOCE_ERR_ARG, "unknown precision %d", precision);
     }
@@ -578,6 +584,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     // update (evolution.c:67,118-126), which moves with the step count
     d.chord = r->precision == VOCE_PREC_MIXED ? g_newton_chord : 0;
     d.nr32 = r->precision == VOCE_PREC_MIXED_NR32;
+    d.ir = r->precision == VOCE_PREC_MIXED_IR;
     for (int p = 0; p < 2; ++p) d.solid[p + 1] = (p < nl->N_phases && !nl->Type_phases[p]) ? 1 : 0;
     d.nsys = sx.nsys;
     d.update_flag = nl->Update_Flag;
@@ -692,7 +699,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     // and precision.
     const long long sm_count = 152;
     long long nb = (nv + 127) / 128;
-    const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(d.nr32 != 0));
+    const long long cap = std::max<long long>(sm_count * 2, nr_resident_blocks(nr_kind(r->precision)));
     r->npart = (int)(nb < cap ? nb : cap);
     d.npart = r->npart;
     int rc = alloc_device(r);
@@ -728,7 +735,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     if (!lu_inv66(S066)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066"); }
     std::memcpy(d.S0, S066, sizeof(S066));
     for (int q = 0; q < 36; ++q) d.S0f[q] = (float)d.S0[q];
-    if (d.nr32) CUDA_TRY(launch_fill_p32(d, r->stream));
+    if (d.nr32 || d.ir) CUDA_TRY(launch_fill_p32(d, r->stream));
     double C0t[81];
     c66_to_t4(&C066[0][0], C0t);
     c66_to_t4(&S066[0][0], d.S0t);
@@ -858,6 +865,7 @@ int make_plan(const std::vector<RveDesc> &descs, int precision, RveDesc *&d_desc
     p.ticks = ticks; p.max_ticks = maxt; p.active_out = act;
     p.mixed = precision != VOCE_PREC_FP64;
     p.nr32 = precision == VOCE_PREC_MIXED_NR32;
+    p.ir = precision == VOCE_PREC_MIXED_IR;
     p.nrve = (int)descs.size();
     if (descs.empty()) return VOCE_OK;
     std::vector<std::vector<int2>> maps(BP_COUNT);
@@ -957,8 +965,11 @@ void read_tile_file()
     TileKey k;
     Tiles t;
     while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d %d %d %d", &k.nx, &k.ny, &k.nz, &k.mixed, &t.zrows,
-                       &t.yxt, &t.xkc, &t.xkc3, &t.zirows, &t.zirows3, &t.sx, &t.sy, &t.sz) == 13)
+                       &t.yxt, &t.xkc, &t.xkc3, &t.zirows, &t.zirows3, &t.sx, &t.sy, &t.sz) == 13) {
+        // the FP64 form runs the default radix schedules whatever the file says
+        if (!k.mixed) t.sx = t.sy = t.sz = 0;
         g_tile_cache[k] = t;
+    }
     std::fclose(f);
 }
 
@@ -1058,8 +1069,12 @@ int autotune_tiles(voce_rve *r)
             }
         }
         // the radix schedule of the axis this phase transforms (z with the
-        // forward z pass, which the inverse one shares), with the chosen tile
-        if (ph == BP_ZI) continue;
+        // forward z pass, which the inverse one shares), with the chosen tile.
+        // The schedule changes the rounding of the transform, so a timed
+        // choice would make results depend on timing noise: the FP64 form
+        // keeps the default schedule of every axis (its bits are the same in
+        // every process), only the single-precision spectrum forms tune it.
+        if (ph == BP_ZI || !d.mixed) continue;
         const int L = ph == BP_ZF ? d.nz : ph == BP_Y6 ? d.ny : d.nx;
         FftPlan1 sc[4];
         const int ns = fft_schedules(L, sc, 4);
@@ -1825,6 +1840,29 @@ void voce_host_free(void *p)
 
 double voce_measure_fp64_tflops(void) { return measure_fp64_tflops(); }
 
+int voce_device_memory(long long *free_bytes, long long *total_bytes)
+{
+    size_t f = 0, t = 0;
+    CUDA_TRY(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = (long long)f;
+    if (total_bytes) *total_bytes = (long long)t;
+    return VOCE_OK;
+}
+
+int voce_diag_rcp(const double *x, double *out, int n)
+{
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(VOCE_ERR_ARG, "bad argument");
+    if (n == 0) return VOCE_OK;
+    double *d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, sizeof(double) * 2 * (size_t)n));
+    cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_rcp_probe(d, d + n, n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "rcp probe: %s", cudaGetErrorString(e));
+    return VOCE_OK;
+}
+
 }  // extern "C"
 
 // ===========================================================================
@@ -1894,6 +1932,7 @@ int build_batch(voce_batch *b)
     p.nrve = n;
     p.mixed = b->precision != VOCE_PREC_FP64;
     p.nr32 = b->precision == VOCE_PREC_MIXED_NR32;
+    p.ir = b->precision == VOCE_PREC_MIXED_IR;
     if (n == 0) { b->dirty = false; return VOCE_OK; }
     std::vector<RveDesc> descs(n);
     for (int i = 0; i < n; ++i) descs[i] = b->rves[i]->d;
@@ -1932,7 +1971,7 @@ int voce_batch_create(int precision, voce_batch **out)
 {
     if (!out) return fail(VOCE_ERR_ARG, "null argument");
     voce_batch *b = new voce_batch();
-    if (precision != VOCE_PREC_FP64 && precision != VOCE_PREC_MIXED && precision != VOCE_PREC_MIXED_NR32) {
+    if (precision < VOCE_PREC_FP64 || precision > VOCE_PREC_MIXED_IR) {
         delete b;
         return fail(VOCE_ERR_ARG, "unknown precision %d", precision);
     }

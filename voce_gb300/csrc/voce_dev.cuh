@@ -87,6 +87,7 @@ struct RveDesc {
     int mixed;           // spectrum precision: 0 double, 1 float
     int chord;           // FP64 Newton: reuse the last Jacobian once the update is below 1e-4
     int nr32;            // Newton iterations in float with an FP64 acceptance step
+    int ir;              // Newton on the FP64 residual with a float Jacobian and solve
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double wgt_ratio;    // wgt / wgt_ph1 (the same IEEE division, once on the host)
     int all_ph1;         // every voxel is phase 1 (the phase-1 sums equal the full ones)
@@ -116,10 +117,11 @@ struct RveDesc {
     double tau0b[VOCE_NS];      // backward CRSS start value
     // fields
     double *sig, *sigp, *eps, *dgs, *dga, *tm, *sch, *sg, *crss, *itau;
-    float *sch32;        // float copy of sch (mixed-precision Newton only)
-    float *itau32;       // float copy of itau (mixed-precision Newton only)
-    float *sgp32;        // float (S_g + S0), packed upper triangle (mixed-precision Newton only)
+    float *sch32;        // float copy of sch (float-Jacobian Newton forms only)
+    float *itau32;       // float copy of itau (float-Jacobian Newton forms only)
+    float *sgp32;        // float (S_g + S0), packed upper triangle (float-Jacobian Newton forms only)
     float *sch_lo, *itau_lo, *sgp_lo;   // x - (double)x32 rounded to float, for the same three
+                                        // (the FP32-Newton form only; null otherwise)
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;
@@ -384,12 +386,12 @@ struct ff32 {
     float h, l;
 };
 
-// stores x as the float pair hi[i] + lo[i]
+// stores x as the float pair hi[i] + lo[i] (hi alone when lo is null)
 __device__ __forceinline__ void put_pair(float *hi, float *lo, long long i, double x)
 {
     const float h = (float)x;
     hi[i] = h;
-    lo[i] = (float)(x - (double)h);
+    if (lo) lo[i] = (float)(x - (double)h);
 }
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)

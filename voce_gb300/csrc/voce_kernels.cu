@@ -181,10 +181,10 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
             for (int c = 0; c < 21; ++c) d.sg[c * nv + v] = 0.0;
             for (int c = 0; c < 60; ++c) d.sch[c * nv + v] = 0.0;
             if (d.sch32)
-                for (int c = 0; c < 60; ++c) { d.sch32[c * nv + v] = 0.0f; d.sch_lo[c * nv + v] = 0.0f; }
+                for (int c = 0; c < 60; ++c) put_pair(d.sch32, d.sch_lo, c * nv + v, 0.0);
             for (int c = 0; c < 24; ++c) { d.crss[c * nv + v] = 0.0; d.itau[c * nv + v] = 0.0; }
             if (d.itau32)
-                for (int c = 0; c < 24; ++c) { d.itau32[c * nv + v] = 0.0f; d.itau_lo[c * nv + v] = 0.0f; }
+                for (int c = 0; c < 24; ++c) put_pair(d.itau32, d.itau_lo, c * nv + v, 0.0);
             continue;
         }
         acc[0] += 1.0;
@@ -789,7 +789,118 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
     }
 }
 
-template <bool NR32, bool CHORD = false>
+// Newton iterations of the VOCE_PREC_MIXED_IR form: every iteration
+// evaluates the reference's residual (evolution.c:78-83, in the symmetric
+// form x = cc + dt edot(s) + (S_g + S0) s) and the flow rule
+// (constitutive.c:126-194: resolved shears, |r|^n, strain rate) in FP64, and
+// takes the stop test of evolution.c:112 in FP64; only the correction -- the
+// Jacobian dt dEdot/ds + S_g + S0 and its LDL^T solve -- is assembled and
+// solved in FP32, from float copies of the Schmid vectors, 1/CRSS and
+// S_g + S0.  This is iterative refinement: each step solves for the FP64
+// residual with an approximate matrix (relative error ~1e-7 times its
+// condition number), so the iteration converges to the root of the FP64
+// residual, near the root nearly as fast as the exact Newton.  A resolved
+// shear ratio |r| >= 60 (where |r|^(n-1) could leave the float range) makes
+// that iteration take the FP64 Jacobian instead.  gam0 is one value for all
+// systems (one slip mode), so it is applied once to the strain-rate sums.
+__device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const double (&P)[21],
+                                          const double (&cc)[6], double thr, double (&sig)[6],
+                                          double (&sp)[6], double (&Rl)[6], int &it)
+{
+    const long long nv = d.nv;
+    const double dtg = d.dt * d.gam0[0];
+    const float dtf = d.dth;
+    const float g1c = d.gam0f[0] * d.nrsf[0];   // gam0 n
+    const int e = d.ipow_n - 1;
+    bool go = true;
+    while (go && it < 100) {
+        ++it;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sp[c] = sig[c];
+        double ed[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        float D[15];
+#pragma unroll
+        for (int q = 0; q < 15; ++q) D[q] = 0.0f;
+        bool big = false;
+        for (int k = 0; k < d.nsys; ++k) {
+            double sc[5];
+#pragma unroll
+            for (int i = 0; i < 5; ++i) sc[i] = __ldg(d.sch + (long long)(5 * k + i) * nv + v);
+            const double rss = sc[0] * sig[0] + sc[1] * sig[1] + sc[2] * sig[2] + sc[3] * sig[3] + sc[4] * sig[4];
+            const int neg = __double2hiint(rss) < 0;
+            const long long ti = (long long)(2 * k + neg) * nv + v;
+            const double r = rss * __ldg(d.itau + ti);
+            const double a = fabs(r);
+            const double ae = pow_abs_e(a, e);        // |r|^(n-1)
+            const double g2 = ae * r;                 // |r|^n sign(r) / gam0
+#pragma unroll
+            for (int i = 0; i < 5; ++i) ed[i] = fma(sc[i], g2, ed[i]);
+            big = big || !(a < 60.0);
+            // Jacobian term gam0 n |r|^(n-1) / tau m m^T, in single precision
+            const float g1 = g1c * (float)ae * __ldg(d.itau32 + ti);
+            float sf[5], t[5];
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                sf[i] = __ldg(d.sch32 + (long long)(5 * k + i) * nv + v);
+                t[i] = g1 * sf[i];
+            }
+            int q = 0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+#pragma unroll
+                for (int j = i; j < 5; ++j) { D[q] = fmaf(t[i], sf[j], D[q]); ++q; }
+        }
+        double R[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            double s = (i < 5) ? fma(dtg, ed[i], cc[i]) : cc[i];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+            R[i] = s;
+            Rl[i] = s;
+        }
+        if (!big) {
+            float M[6][6], x[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                x[i] = (float)R[i];
+#pragma unroll
+                for (int j = 0; j <= i; ++j) {
+                    float m = __ldg(d.sgp32 + (long long)sym6(i, j) * nv + v);
+                    if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    M[i][j] = m;
+                }
+            }
+            ldlt_solve6f(M, x);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
+        } else {
+            double Dd[15], edd[5];
+            flow_rule<true, false, double>(d, v, sig, edd, Dd, nullptr, nullptr);
+            double M[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = 0; j <= i; ++j) {
+                    double m = P[sym6(i, j)];
+                    if (i < 5 && j < 5) m = fma(d.dt, Dd[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    M[i][j] = m;
+                }
+            ldlt_solve6(M, R);
+        }
+        double cnr = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double sn = sig[c] - R[c];
+            const double dd = sn - sig[c];
+            cnr = fma(dd, dd, cnr);
+            sig[c] = sn;
+        }
+        go = cnr > thr;
+    }
+}
+
+template <bool NR32, bool CHORD = false, bool IR = false>
 __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
 {
     // per-thread sums in shared memory (one slot per thread, the same
@@ -864,7 +975,8 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             double P[21];
             load_P(d, v, P);
             // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
-            newton_fp64<false, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            if (IR && d.ipow_n >= 1) newton_ir(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            else newton_fp64<IR, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
         }
         double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
         if (NR32) {
@@ -1523,7 +1635,8 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
 
 // CHORD: the FP64 Newton may take chord steps (VOCE_PREC_MIXED plans; each
 // RVE's d.chord decides); the FP64 form's instance is the exact-Jacobian one
-template <bool NR32, bool CHORD = false>
+// IR: the VOCE_PREC_MIXED_IR form (FP64 residual, float Jacobian)
+template <bool NR32, bool CHORD = false, bool IR = false>
 __global__ void __launch_bounds__(128, NR32 ? VOCE_NR_MIXED_BLOCKS : 1)
 kb_nr(const RveDesc *descs, const int2 *map, int total)
 {
@@ -1531,7 +1644,7 @@ kb_nr(const RveDesc *descs, const int2 *map, int total)
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
         if (!unit_on(d, MASK_ACTIVE)) continue;
-        nr_unit<NR32, CHORD>(d, e.y, d.npart);
+        nr_unit<NR32, CHORD, IR>(d, e.y, d.npart);
     }
 }
 
@@ -1699,17 +1812,19 @@ static const int kNrStageBytes = VOCE_STAGE_FLOATS * VOCE_NR_THREADS * (int)size
 // of kb_nr and the most units an RVE is split into for it.  The first call
 // also raises kb_nr<true>'s dynamic shared-memory limit; it is made when an
 // RVE is created, before any launch or stream capture.
-int nr_resident_blocks(bool nr32)
+int nr_resident_blocks(int kind)
 {
-    static int cached[2] = {0, 0};
-    int &c = cached[nr32 ? 1 : 0];
+    static int cached[3] = {0, 0, 0};
+    int &c = cached[(kind >= 0 && kind < 3) ? kind : 0];
     if (!c) {
         int dev = 0, sms = 152, per = 2;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (nr32) {
+        if (kind == 1) {
             cudaFuncSetAttribute(kb_nr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNrStageBytes);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, VOCE_NR_THREADS, kNrStageBytes);
+        } else if (kind == 2) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false, false, true>, VOCE_NR_THREADS, 0);
         } else {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, VOCE_NR_THREADS, 0);
         }
@@ -1755,13 +1870,16 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     pf.end(K_FFT_Z_INV, s);
     pf.begin(K_NR, s);
     if (bp.nr32)
-        kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(true)), VOCE_NR_THREADS, kNrStageBytes, s>>>(
+        kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(1)), VOCE_NR_THREADS, kNrStageBytes, s>>>(
+            D, bp.map[BP_NP], bp.total[BP_NP]);
+    else if (bp.ir)
+        kb_nr<false, false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(2)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else if (bp.mixed)
-        kb_nr<false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), VOCE_NR_THREADS, 0, s>>>(
+        kb_nr<false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(0)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else
-        kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(false)), VOCE_NR_THREADS, 0, s>>>(
+        kb_nr<false><<<grid_for(bp.total[BP_NP], nr_resident_blocks(0)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     pf.end(K_NR, s);
     pf.begin(K_FIN_ITER, s);
@@ -2001,6 +2119,19 @@ __global__ void k_flush(double *buf, long long n)
 cudaError_t launch_flush(double *buf, long long n, cudaStream_t s)
 {
     k_flush<<<152 * 8, 256, 0, s>>>(buf, n);
+    return cudaGetLastError();
+}
+
+// rcp_nr on n doubles (a check of the Newton step's reciprocal against 1/x)
+__global__ void k_rcp_probe(const double *__restrict__ x, double *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = rcp_nr(x[i]);
+}
+
+cudaError_t launch_rcp_probe(const double *x, double *out, int n, cudaStream_t s)
+{
+    if (n > 0) k_rcp_probe<<<(n + 255) / 256, 256, 0, s>>>(x, out, n);
     return cudaGetLastError();
 }
 

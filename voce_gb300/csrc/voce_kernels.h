@@ -66,6 +66,7 @@ struct BatchPlan {
     int *ticks = nullptr, *max_ticks = nullptr, *active_out = nullptr;
     bool mixed = false;   // float spectrum
     bool nr32 = false;    // float Newton iterations (kb_nr<true>)
+    bool ir = false;      // FP64-residual Newton with a float Jacobian
 };
 // units of one RVE in each phase
 void batch_units(const RveDesc &d, int units[BP_COUNT]);
@@ -97,9 +98,16 @@ cudaError_t launch_voronoi(int nx, int ny, int nz, int ns, const double *seeds, 
 cudaError_t launch_fill_green(const RveDesc &d, cudaStream_t s);
 // the mixed form's float (S_g + S0), once S0 is set in d
 cudaError_t launch_fill_p32(const RveDesc &d, cudaStream_t s);
-// kb_nr blocks resident on the current GPU (SMs x blocks per SM)
-int nr_resident_blocks(bool nr32);
+// Newton-kernel instance of a precision form: 0 FP64 Newton (FP64 and
+// mixed forms), 1 FP32 Newton (mixed_nr32), 2 FP64 residual with an FP32
+// Jacobian (mixed_ir)
+inline int nr_kind(int precision) { return precision == 2 ? 1 : precision == 3 ? 2 : 0; }
+// kb_nr blocks resident on the current GPU (SMs x blocks per SM) for an
+// instance of nr_kind
+int nr_resident_blocks(int kind);
 double measure_fp64_tflops();
+// out[i] = rcp_nr(x[i]) for i < n (device arrays)
+cudaError_t launch_rcp_probe(const double *x, double *out, int n, cudaStream_t s);
 cudaError_t launch_setup(const RveDesc &d, const SetupConst &sc, const double *euler, int npart,
                          cudaStream_t s);
 cudaError_t launch_field_out(const RveDesc &d, int field, double *out, cudaStream_t s);

@@ -129,7 +129,8 @@ int voce_server_create(int precision, long long budget, int ticks_per_round, int
 {
     if (!out || budget <= 0 || ticks_per_round < 1) return VOCE_ERR_ARG;
     voce_server *s = new voce_server();
-    s->precision = (precision == VOCE_PREC_MIXED || precision == VOCE_PREC_MIXED_NR32) ? precision
+    s->precision = (precision == VOCE_PREC_MIXED || precision == VOCE_PREC_MIXED_NR32 ||
+                    precision == VOCE_PREC_MIXED_IR) ? precision
                                                                                       : VOCE_PREC_FP64;
     s->budget = budget;
     s->ticks_per_round = ticks_per_round;
