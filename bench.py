@@ -2,19 +2,32 @@
 
 Workload (one GPU): 64^3 periodic-Voronoi RVE with 125 grains, Cu-like FCC
 crystal, uniaxial tension along z (lateral stresses zero), 2e-4 strain per
-increment, plain FP64.  One step = one strain increment: the prelude, the
-Green-operator fixed-point iterations until the error norms reach Err = 1e-5
-(or IterMax = 200), the increment end.  Metric: voxel-iterations per second
-= sum over steps of (voxels x Green iterations) / time.
+increment, plain FP64.  One step = one whole strain increment: the prelude,
+the Green-operator fixed-point iterations until the error norms reach
+Err = 1e-5 (or IterMax = 200), the increment end.  Metric: voxel-iterations
+per second = sum over steps of (voxels x Green iterations) / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl voce|reference]
-                  [--precision fp64|mixed|mixed_nr32] [--config cfg2|cfg3|cfg4|cfg5]
+                  [--precision fp64|mixed|mixed_ir|mixed_ir_strict|mixed_nr32]
+                  [--config cfg2|cfg3|cfg4|cfg5] [--no-extras]
 
---config cfg3 (256^3 mixed forms vs FP64), cfg4 (batched RVEs), cfg5
-(served requests) are the other workloads' modes; they report every form.
+The default line (cfg2, FP64, N = 1) also carries the metric's other
+numerators, each measured in the same run:
+  forms    config 2 in every precision form (same increments, same timing),
+           with each form's error against the FP64 results;
+  batched  config 4: 512 RVEs in one batch, 2 whole increments each, in the
+           mixed_ir and mixed_nr32 forms, against the plain FP64 path run one
+           RVE at a time;
+  served   config 5 sample: 200 Poisson requests at 100 req/s (increments
+           scaled, stated in the key), served in both forms and by a plain
+           FP64 server that solves one request at a time; p50/p99 latency.
+
+--config cfg3 (256^3, every form vs FP64), cfg4 (batched RVEs), cfg5 (served
+requests) run those workloads alone.
 
 --impl reference times the CPU implementation of the same step (the oracle's
-C restatement of the reference, all host threads) on bounded samples.
+C restatement of the reference, bit-identical to the reference build, all
+host threads) on the same increments: W untimed, then K whole ones timed.
 N > 1 (torchrun): independent replicas, one per GPU, no collective on the
 data path; the time is the max over ranks.
 """
@@ -39,22 +52,32 @@ FLUSH_BYTES = 512 << 20      # > 129 MB L2
 
 def _prec(name):
     from voce_gb300 import capi
-    return {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED,
-            "mixed_nr32": capi.PREC_MIXED_NR32}[name]
+    return {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED, "mixed_ir": capi.PREC_MIXED_IR,
+            "mixed_ir_strict": capi.PREC_MIXED_IR, "mixed_nr32": capi.PREC_MIXED_NR32}[name]
 
 
-PREC = {k: (lambda k=k: _prec(k)) for k in ("fp64", "mixed", "mixed_nr32")}
+FORMS = ("fp64", "mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32")
+PREC = {k: (lambda k=k: _prec(k)) for k in FORMS}
 # the arithmetic types each form computes in
 DTYPE = {"fp64": "f64", "mixed": "f32 spectrum+f64 newton",
+         "mixed_ir": "f32 spectrum+f64 newton residual+f32 newton correction",
+         "mixed_ir_strict": "f32 spectrum+f64 newton residual+f32 newton correction",
          "mixed_nr32": "f32 spectrum+f32 newton+f64 acceptance"}
-FORM_DOC = {"mixed": "FP32 spectrum and Green operator; FP64 Newton, hardening, norms, averages",
-            "mixed_nr32": "as mixed, with FP32 Newton iterations ended by an FP64-residual "
-                          "acceptance step (FP32-only while the Green error is above 1e-4) "
-                          "and FP32 per-voxel error norms"}
-
-
-def _other_mixed(name):
-    return "mixed" if name == "mixed_nr32" else "mixed_nr32"
+FORM_DOC = {"mixed": "FP32 spectrum and Green operator; FP64 Newton (exact Jacobian, chord steps "
+                     "near the root), hardening, norms, averages",
+            "mixed_ir": "FP32 spectrum and Green operator; Newton: FP32 steps choose the start, "
+                        "then every accepted step evaluates the residual and flow rule in FP64 with "
+                        "the FP64 stop test, its Jacobian and LDL^T correction in FP32; hardening, "
+                        "norms, averages in FP64",
+            "mixed_ir_strict": "as mixed_ir without the FP32 start: every Newton step evaluates its "
+                               "residual and flow rule in FP64",
+            "mixed_nr32": "FP32 spectrum and Green operator; FP32 Newton iterations ended by a "
+                          "float-float residual acceptance step (FP32-only while the Green error is "
+                          "above 1e-4); FP32 per-voxel error norms"}
+# whether the form keeps the Newton residual and stop test, the hardening, the
+# averages and the per-voxel convergence norms in FP64 (the precision form's
+# specification); mixed_nr32 does not (FP32 Newton, FP32 norms)
+FORM_SPEC = {"mixed": True, "mixed_ir": True, "mixed_ir_strict": True, "mixed_nr32": False}
 
 
 def parse():
@@ -63,15 +86,24 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="voce", choices=["voce", "reference"])
-    p.add_argument("--precision", default=None, choices=["fp64", "mixed", "mixed_nr32"],
-                   help="default: fp64 (cfg2), mixed_nr32 (cfg3, cfg4, cfg5)")
+    p.add_argument("--precision", default=None, choices=list(FORMS),
+                   help="default: fp64 (cfg2), mixed_ir (cfg3, cfg4, cfg5)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="cfg2: the FP64 line only (no forms / batched / served keys)")
+    p.add_argument("--extra-rves", type=int, default=512, help="cfg2 line: RVEs of the batched key")
+    p.add_argument("--extra-requests", type=int, default=200,
+                   help="cfg2 line: requests of the served key")
+    p.add_argument("--extra-rate", type=float, default=100.0,
+                   help="cfg2 line: arrival rate of the served key, req/s")
+    p.add_argument("--extra-inc-scale", type=float, default=0.025,
+                   help="cfg2 line: served increments per request = max(1, round(scale x U{10..80}))")
     p.add_argument("--rves", type=int, default=512, help="cfg4: RVEs in the batch")
     p.add_argument("--edge", type=int, default=256, help="cfg3: grid edge (radix 2/3 only)")
     p.add_argument("--increments", type=int, default=2,
                    help="cfg4: whole increments every RVE runs in the timed batch")
-    p.add_argument("--requests", type=int, default=32, help="cfg5: requests in the sample")
-    p.add_argument("--rate", type=float, default=2.0, help="cfg5: Poisson arrival rate, req/s")
+    p.add_argument("--requests", type=int, default=200, help="cfg5: requests in the sample")
+    p.add_argument("--rate", type=float, default=100.0, help="cfg5: Poisson arrival rate, req/s")
     p.add_argument("--budget-gb", type=float, default=200.0, help="cfg5: server HBM budget, GB")
     p.add_argument("--active-voxels", type=int, default=4000000,
                    help="cfg5: server active limit, voxels in flight (0: HBM budget alone)")
@@ -79,7 +111,7 @@ def parse():
                    help="cfg5: serve the chosen form only (no other form, no plain FP64 server)")
     p.add_argument("--quantum", type=int, default=0,
                    help="cfg5: ticks after which a running request may be suspended (0: never)")
-    p.add_argument("--inc-scale", type=float, default=0.1,
+    p.add_argument("--inc-scale", type=float, default=0.025,
                    help="cfg5: increments per request = round(scale x U{10..80})")
     p.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"],
                    help="cfg2: the headline line (64^3, FP64); cfg3: 256^3 plane-strain "
@@ -230,66 +262,137 @@ def fp64_flops_per_newton_iteration():
     return KB_NR_FP64_FLOPS_PER_NEWTON, KB_NR_FP64_FLOPS_PER_VOXEL
 
 
-def cpu_sample(threads: int, iters: int):
-    """The oracle (C restatement of the reference) on a bounded sample of
-    the workload: the first increment of the 64^3 case capped at `iters`
-    Green iterations."""
+CFG2_WORKLOAD = ("64^3 periodic Voronoi, 125 grains, Cu FCC (C11=168.4 GPa), n=20, Voce "
+                 "hardening, tension z 1e-3/s, 2e-4 strain per increment (config 2), one whole "
+                 "increment per step")
+
+
+def cfg2_config(nv, iters, precision="fp64"):
+    """The workload keys both arms report: the increments a step runs and
+    their Green-iteration counts (the same for the FP64 GPU path and the
+    CPU reference, which agree iteration for iteration)."""
+    return {"workload": CFG2_WORKLOAD, "precision": precision, "voxels": nv,
+            "green_iterations": iters}
+
+
+def _oracle_job(case, threads):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     if not os.path.exists(orc.PORT_LIB):
         orc.build_port()
-    case = make_case()
-    case.iter_max = iters
     d = tempfile.mkdtemp(prefix="cpu_")
-    nl = case.write(d)
-    j = orc.Job(nl, threads=threads)
+    return orc.Job(case.write(d), threads=threads)
+
+
+def cpu_sample(threads: int, n_incr: int = 2):
+    """The oracle (C restatement of the reference) on a bounded sample of
+    the workload: its first n_incr whole increments, on `threads` threads."""
+    case = make_case()
+    j = _oracle_job(case, threads)
     t0 = time.perf_counter()
-    j.run(1)
+    j.run(n_incr)
     dt = time.perf_counter() - t0
-    n_it = j.increment(0)["iters"]
+    n_it = sum(j.increment(k)["iters"] for k in range(n_incr))
     j.close()
     return case.mesh.nvox * n_it / dt, dt, n_it
 
 
 def run_reference(args, rank, world):
-    """--impl reference: CPU timing of the same step on all host threads."""
+    """--impl reference: the CPU implementation of the same step (the
+    oracle's C restatement of the reference, bit-identical to the reference
+    build) on all host threads: the same W warm-up increments, then the same K
+    whole increments the GPU arm times, each timed alone."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample_iters = 10
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
-    if not os.path.exists(orc.PORT_LIB):
-        orc.build_port()
     case = make_case()
-    case.iter_max = sample_iters
-    d = tempfile.mkdtemp(prefix="ref_")
-    nl = case.write(d)
-    j = orc.Job(nl, threads=threads)
+    nv = case.mesh.nvox
+    j = _oracle_job(case, threads)
     j.run(args.warmup)
-    t0 = time.perf_counter()
-    j.run(args.steps)
-    dt = time.perf_counter() - t0
-    its = sum(j.increment(args.warmup + k)["iters"] for k in range(args.steps))
+    dt = 0.0
+    iters = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        j.run(1)
+        dt += time.perf_counter() - t0
+        iters.append(j.increment(args.warmup + k)["iters"])
     j.close()
-    v = case.mesh.nvox * its / dt
-    sample = ("64^3 Voronoi-125 tension, %d increments capped at %d Green iterations each "
-              "(%d iterations, %.1f s)" % (args.steps, sample_iters, its, dt))
+    v = nv * sum(iters) / dt
+    sample = ("increments %d-%d of the same case, whole (uncapped), after %d untimed ones: "
+              "%d Green iterations, %.1f s on %d threads" % (args.warmup + 1, args.warmup + args.steps,
+                                                            args.warmup, sum(iters), dt, threads))
     out = {
         "impl": "reference", "metric": "voxel_iterations_per_s", "value": v,
         "unit": "voxel-iter/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "64^3 periodic Voronoi, 125 grains, Cu FCC, tension z, "
-                               "FP64, one increment per step (Green iterations capped)",
-                   "cpu_threads": threads},
+        "config": cfg2_config(nv, iters),
         "cpu_baseline": {"value": v, "unit": "voxel-iter/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
+
+
+def _e2e_leg(args, lib, nl, slip, case, prec, grp):
+    """The metric through the C ABI from host buffers: voce_rve_create from
+    pinned host arrays, then K increments, each followed by the stress and
+    strain-rate fields copied to pinned host memory.  It runs first in the
+    process, so it pays what a new caller pays (tile tuning, module loading,
+    graph construction)."""
+    import ctypes as C
+    import numpy as np
+    from voce_gb300 import capi
+    nv = case.mesh.nvox
+    eul_b = lib.voce_host_alloc(nv * 24)
+    gr_b = lib.voce_host_alloc(nv * 4)
+    ph_b = lib.voce_host_alloc(nv * 4)
+    out_b = lib.voce_host_alloc(2 * nv * 48)
+    eul = np.ctypeslib.as_array((C.c_double * (nv * 3)).from_address(eul_b)).reshape(nv, 3)
+    gr = np.ctypeslib.as_array((C.c_int * nv).from_address(gr_b))
+    ph = np.ctypeslib.as_array((C.c_int * nv).from_address(ph_b))
+    outs = np.ctypeslib.as_array((C.c_double * (2 * nv * 6)).from_address(out_b)).reshape(2, 6 * nv)
+    eul[:] = case.mesh.euler_deg
+    gr[:] = case.mesh.grain
+    ph[:] = case.mesh.phase
+    grp.barrier()
+    t0 = time.perf_counter()
+    re = capi.Rve.create(nl, slip, eul, gr, ph, prec)
+    e2e_iters = 0
+    for k in range(args.steps):
+        re.run(1)
+        e2e_iters += re.increment(k)["iters"]
+        lib.voce_rve_get_field(re._h, 20, outs[0].ctypes.data_as(C.POINTER(C.c_double)))
+        lib.voce_rve_get_field(re._h, 21, outs[1].ctypes.data_as(C.POINTER(C.c_double)))
+    re.close()
+    t_e2e = time.perf_counter() - t0
+    grp.barrier()
+    t_e2e = grp.max(t_e2e)
+    for b in (eul_b, gr_b, ph_b, out_b):
+        lib.voce_host_free(b)
+    return {"value": grp.sum(float(nv * e2e_iters)) / t_e2e, "unit": "voxel-iter/s",
+            "h2d_bytes_per_step": int(nv * 32 / args.steps),
+            "d2h_bytes_per_step": int(2 * 6 * 8 * nv),
+            "timed": "create from pinned host mesh (first in the process: tile tuning and "
+                     "graph construction included) + %d increments, each followed by the stress "
+                     "and strain-rate fields copied to pinned host memory" % args.steps}
+
+
+def _timed_increments(r, warmup, steps):
+    """K increments after W, each timed with CUDA events on the RVE's stream
+    after an L2 flush; returns (ms list, Green iterations list, Newton
+    iterations summed)."""
+    r.run(warmup)
+    step_ms, iters, nr = [], [], 0.0
+    for k in range(steps):
+        r.flush_l2(FLUSH_BYTES)
+        step_ms.append(r.run_timed(1))
+        inc = r.increment(warmup + k)
+        iters.append(inc["iters"])
+        nr += inc["nr_iters_total"]
+    return step_ms, iters, nr
 
 
 def run_voce(args, rank, world, grp):
@@ -303,6 +406,9 @@ def run_voce(args, rank, world, grp):
     nl_path = case.write(d)
     nl = capi.read_namelist(nl_path)
     slip = capi.read_slip(os.path.join(d, "mat.sx"))
+
+    # ---- end-to-end leg through the C ABI, host buffers (first) ---------
+    e2e = None if args.no_e2e else _e2e_leg(args, lib, nl, slip, case, prec, grp)
 
     # ---- device-resident leg: K increments timed with CUDA events --------
     # Each increment runs as one CUDA graph (device-side conditional loop
@@ -326,6 +432,8 @@ def run_voce(args, rank, world, grp):
     launches = r.kernel_launches - launches0
     tot_ms = sum(step_ms)
     value, t_max, vox_iters = whole_job_rate(grp, float(nv * sum(iters)), tot_ms)
+    fp64_ref = {"incs": [r.increment(k) for k in range(args.warmup + args.steps)],
+                "sig": r.field("sig_voigt"), "edot": r.field("edot_voigt"), "iters": iters}
 
     # ---- per-kernel durations: CUDA events around every launch over the
     # next few increments (host-driven loop, same kernels, same stream) ----
@@ -348,66 +456,37 @@ def run_voce(args, rank, world, grp):
     fp64_ach = ((fpi[0] * prof_nr_iters + fpi[1] * nv * nr_n) / (nr_ms * 1e-3) / 1e12) if fpi else None
     r.close()
 
-    # ---- end-to-end leg through the C ABI, host buffers ----------------
-    e2e = None
-    if not args.no_e2e:
-        import ctypes as C
-        import numpy as np
-        eul_b = lib.voce_host_alloc(nv * 24)
-        gr_b = lib.voce_host_alloc(nv * 4)
-        ph_b = lib.voce_host_alloc(nv * 4)
-        out_b = lib.voce_host_alloc(2 * nv * 48)
-        eul = np.ctypeslib.as_array((C.c_double * (nv * 3)).from_address(eul_b)).reshape(nv, 3)
-        gr = np.ctypeslib.as_array((C.c_int * nv).from_address(gr_b))
-        ph = np.ctypeslib.as_array((C.c_int * nv).from_address(ph_b))
-        outs = np.ctypeslib.as_array((C.c_double * (2 * nv * 6)).from_address(out_b)).reshape(2, 6 * nv)
-        eul[:] = case.mesh.euler_deg
-        gr[:] = case.mesh.grain
-        ph[:] = case.mesh.phase
-        grp.barrier()
-        t0 = time.perf_counter()
-        re = capi.Rve.create(nl, slip, eul, gr, ph, prec)
-        e2e_iters = 0
-        for k in range(args.steps):
-            re.run(1)
-            e2e_iters += re.increment(k)["iters"]
-            lib.voce_rve_get_field(re._h, 20, outs[0].ctypes.data_as(C.POINTER(C.c_double)))
-            lib.voce_rve_get_field(re._h, 21, outs[1].ctypes.data_as(C.POINTER(C.c_double)))
-        re.close()
-        t_e2e = time.perf_counter() - t0
-        grp.barrier()
-        t_e2e = grp.max(t_e2e)
-        e2e = {"value": grp.sum(float(nv * e2e_iters)) / t_e2e, "unit": "voxel-iter/s",
-               "h2d_bytes_per_step": int(nv * 32 / args.steps),
-               "d2h_bytes_per_step": int(2 * 6 * 8 * nv),
-               "timed": "create from pinned host mesh + %d increments, each followed by the "
-                        "stress and strain-rate fields copied to pinned host memory" % args.steps}
-        for b in (eul_b, gr_b, ph_b, out_b):
-            lib.voce_host_free(b)
-
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        v, dt, n_it = cpu_sample(threads, 40)
+        v, dt, n_it = cpu_sample(threads, 2)
         cpu = {"value": v, "unit": "voxel-iter/s", "cores": threads, "kind": "port",
-               "sample": "first increment of the same 64^3 case capped at %d Green iterations "
-                         "(%.1f s on %d threads)" % (n_it, dt, threads)}
+               "sample": "the first 2 whole increments of the same 64^3 case (%d Green iterations, "
+                         "%.1f s on %d threads); --impl reference times the increments this line "
+                         "times" % (n_it, dt, threads)}
+
+    # ---- the precision, batched and served forms (N=1 only) ------------
+    extras = {}
+    if world == 1 and not args.no_extras and args.precision == "fp64":
+        extras["forms"] = forms_cfg2(args, nl, slip, case, value, fp64_ref)
+        extras["batched"] = cfg4_core(args.extra_rves, args.increments, ("mixed_ir", "mixed_nr32"))
+        extras["served"] = cfg5_core(args.extra_requests, args.extra_rate, args.extra_inc_scale,
+                                     ("mixed_ir", "mixed_nr32"), plain=True, budget_gb=args.budget_gb,
+                                     active_voxels=args.active_voxels, quantum=0)
 
     if rank != 0:
         return
+    conf = cfg2_config(nv, iters, args.precision)
+    conf.update({"l2": "flushed (512 MB write) before every step",
+                 "parallelism": "replicas" if world > 1 else "single GPU"})
     out = {
         "metric": "voxel_iterations_per_s", "value": value, "unit": "voxel-iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPE[args.precision],
         "data": "synthetic",
-        "config": {"workload": "64^3 periodic Voronoi, 125 grains, Cu FCC (C11=168.4 GPa), "
-                               "n=20, Voce hardening, tension z 1e-3/s, 2e-4 strain per "
-                               "increment (config 2), one increment per step",
-                   "precision": args.precision, "voxels": nv,
-                   "green_iterations": iters, "l2": "flushed (512 MB write) before every step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": conf,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(args.precision),
                      "kernel": "kb_nr", "peak_kind": peak_kind,
@@ -426,7 +505,54 @@ def run_voce(args, rank, world, grp):
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    out.update(extras)
     print(json.dumps(out), flush=True)
+
+
+def _rel(x, y):
+    import numpy as np
+    x = np.asarray(x, float)
+    y = np.asarray(y, float)
+    return float(np.abs(x - y).max() / np.abs(y).max())
+
+
+def forms_cfg2(args, nl, slip, case, fp64_value, fp64_ref):
+    """Config 2 in every precision form: the same W + K increments as the
+    FP64 leg, K of them timed the same way; each form's rate against the FP64
+    line's and its error against the FP64 results of the same increments."""
+    from voce_gb300 import capi
+    lib = capi.load()
+    nv = case.mesh.nvox
+    out = {}
+    for name in ("mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32"):
+        lib.voce_set_ir_predictor(0 if name == "mixed_ir_strict" else 1)
+        try:
+            r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase,
+                                PREC[name]())
+        finally:
+            lib.voce_set_ir_predictor(1)
+        step_ms, iters, nr = _timed_increments(r, args.warmup, args.steps)
+        incs = [r.increment(k) for k in range(args.warmup + args.steps)]
+        sig, edot = r.field("sig_voigt"), r.field("edot_voigt")
+        r.set_profiling(True)
+        r.reset_kernel_times()
+        r.run(1)
+        n_it = r.increment(args.warmup + args.steps)["iters"]
+        kus = {k: round(1e3 * t / n_it, 1) for k, (t, n) in r.kernel_times().items() if n > 0}
+        r.close()
+        v = nv * sum(iters) / (sum(step_ms) * 1e-3)
+        out[name] = {
+            "value": v, "over_fp64": v / fp64_value, "ms_per_step": sum(step_ms) / args.steps,
+            "arithmetic": FORM_DOC[name], "within_precision_spec": FORM_SPEC[name],
+            "newton_iterations_per_voxel_iteration": nr / (nv * sum(iters)),
+            "kernel_us_per_iteration": kus,
+            "error_vs_fp64": {
+                "macro_stress_max_rel": max(_rel(x["sig_avg"], y["sig_avg"])
+                                            for x, y in zip(incs, fp64_ref["incs"])),
+                "sigma_field_max_rel": _rel(sig, fp64_ref["sig"]),
+                "edot_field_max_rel": _rel(edot, fp64_ref["edot"]),
+                "green_iterations": [iters, fp64_ref["iters"]]}}
+    return out
 
 
 def run_cfg3(args):
@@ -436,7 +562,7 @@ def run_cfg3(args):
     form --precision names (default mixed_nr32)."""
     import numpy as np
     from voce_gb300 import capi, synth
-    chosen = args.precision or "mixed_nr32"
+    chosen = args.precision or "mixed_ir"
     t0 = time.perf_counter()
     # config 3 (synth.config3), its mesh tessellated on the GPU
     case = synth.Case("cfg3_%d" % args.edge, _voronoi_mesh(args.edge, 4096, 3), synth.CU_LIKE,
@@ -450,9 +576,14 @@ def run_cfg3(args):
     slip = capi.read_slip(os.path.join(d, "mat.sx"))
     nv = case.mesh.nvox
     out = {}
-    for name in ("fp64", "mixed", "mixed_nr32"):
-        r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase,
-                            PREC[name]())
+    lib = capi.load()
+    for name in ("fp64", "mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32"):
+        lib.voce_set_ir_predictor(0 if name == "mixed_ir_strict" else 1)
+        try:
+            r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase,
+                                PREC[name]())
+        finally:
+            lib.voce_set_ir_predictor(1)
         r.run(args.warmup)
         ms, its = 0.0, 0
         for k in range(args.steps):
@@ -480,12 +611,13 @@ def run_cfg3(args):
     b = out["fp64"]
     forms = {"fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"],
                       "kernel_us_per_iteration": b["kernel_us_per_iteration"]}}
-    for name in ("mixed", "mixed_nr32"):
+    for name in ("mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32"):
         a = out[name]
         forms[name] = {
             "value": a["value"], "ms_per_step": a["ms"] / args.steps, "iters": a["iters"],
             "kernel_us_per_iteration": a["kernel_us_per_iteration"],
             "over_fp64": a["value"] / b["value"], "arithmetic": FORM_DOC[name],
+            "within_precision_spec": FORM_SPEC[name],
             "error_vs_fp64": {
                 "macro_stress_max_rel": max(rel(x["sig_avg"], y["sig_avg"])
                                             for x, y in zip(a["incs"], b["incs"])),
@@ -552,28 +684,35 @@ def _plain_class_throughput(cases_by_edge, d):
     return thr
 
 
-def run_cfg4(args):
-    """Batched form: RVEs with edges drawn from {16,32,48,64}, grains
-    log-uniform 8-512, random traceless loads, 2.5e-4 per increment, advanced
-    in one batch (one launch per phase per tick, the tick loop a CUDA graph),
-    in both mixed forms; `value` is the form --precision names (default
-    mixed_nr32).  Bounded sample: `--increments` whole increments of every
-    RVE (the batch runs until the last RVE finishes them).  Accuracy: one
-    RVE of each edge run through a whole increment in a batch of each form,
-    against the FP64 form alone."""
+def _cfg4_cases(n_rves):
     import numpy as np
-    from voce_gb300 import capi, synth
-    chosen = args.precision or "mixed_nr32"
+    from voce_gb300 import synth
     rng = np.random.Generator(np.random.PCG64(4))
-    d = tempfile.mkdtemp(prefix="cfg4_")
-    t0 = time.perf_counter()
     cases = []
-    for i in range(args.rves):
+    for i in range(n_rves):
         edge = int(rng.choice([16, 32, 48, 64]))
         grains = _loguniform_int(rng, 8, 512)
         load = synth.random_traceless_load(rng)
         mesh = _voronoi_mesh(edge, grains, 10000 + i)
         cases.append(synth.Case("b%d" % i, mesh, synth.CU_LIKE, load, 0.25, 40))
+    return cases
+
+
+def cfg4_core(n_rves, increments, forms):
+    """Batched form (config 4): n_rves RVEs with edges drawn from
+    {16,32,48,64}, grains log-uniform 8-512, random traceless loads, 2.5e-4
+    per increment, advanced in one batch per form (one launch per phase per
+    tick, the tick loop a CUDA graph).  Every RVE runs `increments` whole
+    increments; the timed region ends when the last finishes.  Against the
+    plain FP64 path run one RVE at a time (per-edge rates measured on a whole
+    increment, weighted by the sample's voxels).  Accuracy: one RVE per edge
+    through a whole first increment in a batch of each form, against the FP64
+    form alone."""
+    import numpy as np
+    from voce_gb300 import capi
+    d = tempfile.mkdtemp(prefix="cfg4_")
+    t0 = time.perf_counter()
+    cases = _cfg4_cases(n_rves)
     t_gen = time.perf_counter() - t0
     nv_tot = sum(c.mesh.nvox for c in cases)
     inputs = [_rve_inputs(c, d, str(i)) for i, c in enumerate(cases)]
@@ -581,36 +720,35 @@ def run_cfg4(args):
     def create(c, inp, prec):
         return capi.Rve.create(inp[0], inp[1], c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, prec)
 
-    forms = {}
+    out = {}
     kernel_ms = {}
-    for name in (chosen, _other_mixed(chosen)):
+    for name in forms:
         prec = PREC[name]()
         t0 = time.perf_counter()
         rves = [create(c, inp, prec) for c, inp in zip(cases, inputs)]
         t_setup = time.perf_counter() - t0
         b = capi.Batch(prec)
         for r in rves:
-            b.add(r, args.increments)
+            b.add(r, increments)
         warm = 3
         b.run(max_ticks=warm)                         # warm-up (graph build)
         assert all(r.increments_done == 0 for r in rves)
         t0 = time.perf_counter()
-        ticks = 0
-        while True:
-            left = b.run(max_ticks=50)
-            if left == 0:
-                break
+        while b.run(max_ticks=50):
+            pass
         t_run = time.perf_counter() - t0
         ticks = b.ticks - warm
         # voxel-iterations of the timed region: every Green iteration of the
         # whole increments, less the warm-up ticks (all RVEs active then)
-        vi = sum(r.nv * r.increment(k)["iters"] for r in rves for k in range(args.increments))
+        vi = sum(r.nv * r.increment(k)["iters"] for r in rves for k in range(increments))
         vi -= warm * nv_tot
-        forms[name] = {"value": vi / t_run, "seconds": t_run, "ticks": ticks,
-                       "ms_per_tick": 1e3 * t_run / ticks, "voxel_iterations": vi,
-                       "setup_s": t_setup, "arithmetic": FORM_DOC[name]}
+        out[name] = {"value": vi / t_run, "seconds": t_run, "ticks": ticks,
+                     "ms_per_tick": 1e3 * t_run / ticks, "voxel_iterations": vi,
+                     "setup_s": t_setup, "arithmetic": FORM_DOC[name],
+                     "within_precision_spec": FORM_SPEC[name],
+                     "hbm_gb": sum(capi.footprint(c.mesh.dims, prec) for c in cases) / 1e9}
         b.close()
-        if name == chosen:
+        if name == forms[0]:
             # per-phase breakdown: ticks of one more increment of every RVE,
             # driven from the host with every launch timed (after the timed
             # region)
@@ -639,71 +777,77 @@ def run_cfg4(args):
         for (edge, (c, inp)), r in zip(sample.items(), rves):
             with create(c, inp, capi.PREC_FP64) as rr:
                 rr.run(1)
-                x = np.array(r.increment(0)["sig_avg"])
-                y = np.array(rr.increment(0)["sig_avg"])
-                errs[str(edge)] = float(np.abs(x - y).max() / np.abs(y).max())
+                errs[str(edge)] = _rel(r.increment(0)["sig_avg"], rr.increment(0)["sig_avg"])
             r.close()
-        forms[name]["first_increment_macro_stress_err_vs_fp64"] = errs
+        out[name]["first_increment_macro_stress_err_vs_fp64"] = errs
     by_edge = {e: c for e, (c, _) in sample.items()}
     thr = _plain_class_throughput(by_edge, d)
     t_plain = sum(c.mesh.nvox / thr[c.mesh.dims[0]] for c in cases)   # per iteration of all RVEs
     plain = nv_tot / t_plain
-    for f in forms.values():
+    for f in out.values():
         f["batched_over_plain"] = f["value"] / plain
-    a = forms[chosen]
-    res = {
+    return {"workload": "batched: %d RVEs, edges U{16,32,48,64}, grains log-U[8,512], random "
+                        "traceless loads 1e-3/s, 2.5e-4 per increment (config 4), %d whole "
+                        "increments per RVE" % (len(cases), increments),
+            "rves": len(cases), "voxels": nv_tot, "mesh_generation_s": t_gen,
+            "plain_fp64_one_at_a_time": {"value": plain, "per_edge": thr},
+            "forms": out, "kernel_ms_per_tick": {forms[0]: kernel_ms},
+            "kernel_timing": "CUDA events around every launch of 5 host-driven ticks of one more "
+                             "increment of every RVE, after the timed region"}
+
+
+def run_cfg4(args):
+    """--config cfg4: the batched form alone; `value` is the form --precision
+    names (default mixed_ir), the other form beside it."""
+    chosen = args.precision or "mixed_ir"
+    other = "mixed_nr32" if chosen != "mixed_nr32" else "mixed_ir"
+    res = cfg4_core(args.rves, args.increments, (chosen, other))
+    a = res["forms"][chosen]
+    line = {
         "metric": "voxel_iterations_per_s", "value": a["value"], "unit": "voxel-iter/s", "n_gpus": 1,
         "steps": a["ticks"], "warmup": 3, "ms_per_step": a["ms_per_tick"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[chosen],
         "data": "synthetic",
-        "config": {"workload": "batched: %d RVEs, edges U{16,32,48,64}, grains log-U[8,512], "
-                               "random traceless loads 1e-3/s, 2.5e-4 per increment (config 4), "
-                               "%s form, %d whole increments per RVE, one batch tick per "
-                               "step" % (len(cases), chosen, args.increments),
-                   "voxels": nv_tot, "mesh_generation_s": t_gen,
-                   "l2": "inputs larger than L2 (%.1f GB of RVE state)" % (
-                       sum(capi.footprint(c.mesh.dims, PREC[chosen]()) for c in cases) / 1e9)},
-        "plain_fp64_one_at_a_time": {"value": plain, "per_edge": thr},
+        "config": {"workload": res["workload"] + ", %s form, one batch tick per step" % chosen,
+                   "voxels": res["voxels"],
+                   "l2": "inputs larger than L2 (%.1f GB of RVE state)" % a["hbm_gb"]},
         "batched_over_plain": a["batched_over_plain"],
-        "forms": forms,
-        "kernel_ms_per_tick": kernel_ms,
-        "kernel_timing": "CUDA events around every launch of 5 host-driven ticks of one more "
-                         "increment of every RVE, after the timed region",
     }
-    print(json.dumps(res), flush=True)
+    line.update(res)
+    print(json.dumps(line), flush=True)
 
 
-def run_cfg5(args):
-    """Serving form: Poisson arrivals of RVE solve requests (edges
-    U{16,32,64,128}, grains log-U[8,2048], random traceless loads), served
-    with continuous batching in both mixed forms, against a plain-FP64 server
-    that solves one request at a time, on the same arrival trace."""
+def cfg5_core(n_requests, rate, inc_scale, forms, plain=True, budget_gb=200.0,
+              active_voxels=4000000, quantum=0):
+    """Serving form (config 5): Poisson arrivals of RVE solve requests (edges
+    U{16,32,64,128}, grains log-U[8,2048], random traceless loads,
+    increments max(1, round(inc_scale x U{10..80}))), served with continuous
+    batching in each form, against a plain-FP64 server that solves one
+    request at a time, on the same arrival trace."""
     import numpy as np
     from voce_gb300 import capi, synth
     rng = np.random.Generator(np.random.PCG64(5))
     d = tempfile.mkdtemp(prefix="cfg5_")
     reqs = []
     t_arr = 0.0
-    for i in range(args.requests):
-        t_arr += rng.exponential(1.0 / args.rate)
+    t0 = time.perf_counter()
+    for i in range(n_requests):
+        t_arr += rng.exponential(1.0 / rate)
         edge = int(rng.choice([16, 32, 64, 128]))
         grains = _loguniform_int(rng, 8, 2048)
         load = synth.random_traceless_load(rng)
-        inc = max(1, int(round(args.inc_scale * rng.integers(10, 81))))
+        inc = max(1, int(round(inc_scale * rng.integers(10, 81))))
         mesh = _voronoi_mesh(edge, min(grains, edge ** 3), 20000 + i)
         c = synth.Case("q%d" % i, mesh, synth.CU_LIKE, load, 0.2, inc)
         nl, sx = _rve_inputs(c, d, str(i))
         reqs.append((t_arr, c, nl, sx, inc))
-
-    preempt = [0]
+    t_gen = time.perf_counter() - t0
 
     def serve(precision, one_at_a_time):
-        preempt[0] = 0
-        budget = int(args.budget_gb * (1 << 30))
-        lat, vi = [], 0
+        budget = int(budget_gb * (1 << 30))
+        lat, vi, pre = [], 0, 0
         t0 = time.perf_counter()
         if one_at_a_time:
-            clock = 0.0
             for (ta, c, nl, sx, inc) in reqs:
                 wait = ta - (time.perf_counter() - t0)
                 if wait > 0:
@@ -714,11 +858,10 @@ def run_cfg5(args):
                 r.field("sig_voigt")
                 r.close()
                 lat.append((time.perf_counter() - t0) - ta)
-            span = time.perf_counter() - t0
-            return lat, vi, span
+            return lat, vi, time.perf_counter() - t0, 0
         with capi.Server(precision, budget, ticks_per_round=16) as s:
-            s.set_quantum(args.quantum)
-            s.set_active_limit(args.active_voxels)
+            s.set_quantum(quantum)
+            s.set_active_limit(active_voxels)
             ids = []
             k = 0
             while True:
@@ -741,42 +884,53 @@ def run_cfg5(args):
                 # arrival -> done: time in the server plus the poll delay before submission
                 lat.append((info.t_done - info.t_submit) + (sub_wall - ta))
                 vi += info.voxel_iterations
-                preempt[0] += info.preemptions
-        return lat, vi, span
+                pre += info.preemptions
+        return lat, vi, span, pre
 
-    chosen = args.precision or "mixed_nr32"
     out = {}
-    runs = (("served_" + chosen, PREC[chosen](), False),
-            ("served_" + _other_mixed(chosen), PREC[_other_mixed(chosen)](), False),
-            ("plain_fp64_one_at_a_time", capi.PREC_FP64, True))
-    for name, prec, single in runs[:1] if args.served_only else runs:
-        lat, vi, span = serve(prec, single)
+    runs = [("served_" + f, PREC[f](), False) for f in forms]
+    if plain:
+        runs.append(("plain_fp64_one_at_a_time", capi.PREC_FP64, True))
+    for name, prec, single in runs:
+        lat, vi, span, pre = serve(prec, single)
         out[name] = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                      "throughput": vi / span, "makespan_s": span, "voxel_iterations": vi}
         if not single:
-            out[name]["preemptions"] = preempt[0]
+            out[name].update(preemptions=pre, within_precision_spec=FORM_SPEC[name[7:]])
     b = out.get("plain_fp64_one_at_a_time")
     for name, a in out.items():
         if b is not None and name != "plain_fp64_one_at_a_time":
             a.update(throughput_ratio=a["throughput"] / b["throughput"],
                      p50_ratio=b["p50_s"] / a["p50_s"], p99_ratio=b["p99_s"] / a["p99_s"])
-    a = out["served_" + chosen]
-    res = {
+    return {"workload": "serving: %d Poisson requests at %.1f req/s, edges U{16,32,64,128}, grains "
+                        "log-U[8,2048], random traceless loads, increments max(1, round(%.3g x "
+                        "U{10..80})) (config 5 sample), continuous batching" % (
+                            len(reqs), rate, inc_scale),
+            "requests": len(reqs), "arrival_rate_per_s": rate, "increment_scale": inc_scale,
+            "hbm_budget_gb": budget_gb, "active_limit_voxels": active_voxels,
+            "quantum_ticks": quantum, "request_generation_s": t_gen, "runs": out}
+
+
+def run_cfg5(args):
+    """--config cfg5: the served forms alone; `value` is the form --precision
+    names (default mixed_ir)."""
+    chosen = args.precision or "mixed_ir"
+    forms = (chosen,) if args.served_only else (chosen, "mixed_nr32" if chosen != "mixed_nr32" else "mixed_ir")
+    res = cfg5_core(args.requests, args.rate, args.inc_scale, forms, plain=not args.served_only,
+                    budget_gb=args.budget_gb, active_voxels=args.active_voxels, quantum=args.quantum)
+    a = res["runs"]["served_" + chosen]
+    line = {
         "metric": "voxel_iterations_per_s", "value": a["throughput"], "unit": "voxel-iter/s",
-        "n_gpus": 1, "steps": len(reqs), "warmup": 0, "ms_per_step": 1e3 * a["makespan_s"] / len(reqs),
+        "n_gpus": 1, "steps": res["requests"], "warmup": 0,
+        "ms_per_step": 1e3 * a["makespan_s"] / res["requests"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[chosen],
         "data": "synthetic",
-        "config": {"workload": "serving: %d Poisson requests at %.2f req/s, edges U{16,32,64,128}, "
-                               "grains log-U[8,2048], random traceless loads, increments "
-                               "round(%.2f x U{10..80}) (config 5 sample), continuous batching, "
-                               "%s form" % (len(reqs), args.rate, args.inc_scale, chosen),
-                   "hbm_budget_gb": args.budget_gb, "quantum_ticks": args.quantum,
-                   "active_limit_voxels": args.active_voxels},
-        "served": out,
+        "config": {"workload": res["workload"] + ", %s form" % chosen},
         "throughput_ratio": a.get("throughput_ratio"), "p50_ratio": a.get("p50_ratio"),
         "p99_ratio": a.get("p99_ratio"),
     }
-    print(json.dumps(res), flush=True)
+    line.update(res)
+    print(json.dumps(line), flush=True)
 
 
 def main():

@@ -50,7 +50,9 @@ enum {
     VOCE_ERR_UNSUPPORTED = 6, /* grid size or material this build does not handle */
     VOCE_ERR_NOMEM = 7,       /* device allocation failed */
     VOCE_ERR_CUDA = 8,        /* CUDA runtime error, or no GPU */
-    VOCE_ERR_STATE = 9        /* call out of order */
+    VOCE_ERR_STATE = 9,       /* call out of order */
+    VOCE_ERR_CANCELLED = 10,  /* request cancelled by the caller (voce_serve.h) */
+    VOCE_ERR_DEADLINE = 11    /* request not done by its deadline (voce_serve.h) */
 };
 
 /* Precision forms.
@@ -65,14 +67,16 @@ enum {
  *                         norms in FP32 (their sums in FP64).  The Newton
  *                         iterations and the norms are not FP64 here.
  *   VOCE_PREC_MIXED_IR    spectrum and Green-operator convolution in FP32;
- *                         every Newton iteration evaluates the residual and
- *                         the flow rule (resolved shears, power law, strain
- *                         rate) in FP64 and takes its stop test in FP64, and
- *                         only the correction -- the Jacobian's assembly and
- *                         its LDL^T solve -- is FP32 (iterative refinement:
- *                         the converged stress is the root of the FP64
- *                         residual); hardening, averages and the per-voxel
- *                         error norms in FP64. */
+ *                         the Newton iterations that accept a stress
+ *                         evaluate the residual and the flow rule (resolved
+ *                         shears, power law, strain rate) in FP64 and take
+ *                         the reference's stop test in FP64, with the
+ *                         correction -- the Jacobian's assembly and its LDL^T
+ *                         solve -- in FP32 (iterative refinement: the
+ *                         accepted stress is a root of the FP64 residual);
+ *                         they start from a point solved on the FP32 pipe
+ *                         (voce_set_ir_predictor); hardening, averages and
+ *                         the per-voxel error norms in FP64. */
 enum { VOCE_PREC_FP64 = 0, VOCE_PREC_MIXED = 1, VOCE_PREC_MIXED_NR32 = 2, VOCE_PREC_MIXED_IR = 3 };
 
 /* Every variable the reference's namelist reader knows (io.c:25-52), with

@@ -83,7 +83,8 @@ int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
  * different order of roundings).  So the FP64 form never tunes it: its RVEs
  * run the default schedule of every axis unless the caller sets one, and its
  * results are the same bits in every process.  For the single-precision
- * spectrum forms (VOCE_PREC_MIXED, VOCE_PREC_MIXED_NR32), with tuning on,
+ * spectrum forms (VOCE_PREC_MIXED, VOCE_PREC_MIXED_NR32, VOCE_PREC_MIXED_IR),
+ * with tuning on,
  * voce_rve_create times the candidates of each axis on the forward pass that
  * transforms it (with the tuned tile) and keeps one only when it is more than
  * 3 % faster than the default; the choice is cached with the tiles (and in
@@ -109,6 +110,18 @@ int voce_fft_schedule_count(int L);
  * the FP64 form's parity bound, so the FP64 form never takes chord steps.
  * On (1) by default; applies to RVEs created afterwards. */
 int voce_set_newton_chord(int on);
+/* Start of the VOCE_PREC_MIXED_IR Newton (no counterpart in the reference):
+ * before its FP64-residual iterations, each voxel's stress is moved from the
+ * Green iterate by Newton steps computed on the FP32 pipe -- single-precision
+ * steps to a relative update of 1e-4, then one step on a float-float residual
+ * (about 48 bits) -- to within about 1e-9 relative of the FP64 residual's
+ * root.  The FP64-residual steps and their stop test (evolution.c:112) then
+ * run unchanged, so every accepted stress is a root of the FP64 residual to
+ * the same test, and the strain rate is evaluated at the FP64 iteration's
+ * start; the start only shortens the FP64 iterations (usually to one step).
+ * Off, every Newton step of the form evaluates its residual in FP64 from the
+ * Green iterate.  On (1) by default; applies to RVEs created afterwards. */
+int voce_set_ir_predictor(int on);
 int voce_rve_get_fft_schedule(const voce_rve *r, int axis, int *radices, int max);
 int voce_rve_set_fft_schedule(voce_rve *r, int axis, int k);
 

@@ -12,6 +12,14 @@
  * admissions.  Requests that arrive while others run join the running batch
  * at the next round; fields and hardening state stay on the device between
  * increments.  Times are seconds on the server's monotonic clock.
+ *
+ * A request can be cancelled, and given a deadline, at any time between
+ * calls: a cancelled request leaves the queue, or the running batch between
+ * two ticks, and its device memory is freed at once; a request that is not
+ * done by its deadline is ended the same way at the start of the next
+ * voce_server_poll, with the error VOCE_ERR_DEADLINE.  Neither changes the
+ * other requests' results (each RVE's arithmetic is independent of what else
+ * is in the batch).
  */
 #ifndef VOCE_SERVE_H
 #define VOCE_SERVE_H
@@ -24,7 +32,8 @@ extern "C" {
 
 typedef struct voce_server voce_server;
 
-enum { VOCE_REQ_QUEUED = 0, VOCE_REQ_RUNNING = 1, VOCE_REQ_DONE = 2, VOCE_REQ_FAILED = 3 };
+enum { VOCE_REQ_QUEUED = 0, VOCE_REQ_RUNNING = 1, VOCE_REQ_DONE = 2, VOCE_REQ_FAILED = 3,
+       VOCE_REQ_CANCELLED = 4 };
 
 typedef struct {
     long long id;
@@ -36,6 +45,7 @@ typedef struct {
     long long voxel_iterations; /* sum over its increments of voxels x Green iterations */
     voce_increment last;        /* record of its last increment */
     int preemptions;            /* times it was suspended to make room */
+    double t_deadline;          /* server time by which it must be done (0: none) */
 } voce_request_info;
 
 /* keep_fields: keep the final stress and strain-rate fields (Voigt order,
@@ -62,7 +72,18 @@ int voce_server_set_quantum(voce_server *s, int ticks);
  * and lets requests finish in arrival order, which lowers p50 and p99
  * latency.  0 (the default): admission by HBM footprint alone. */
 int voce_server_set_active_limit(voce_server *s, long long voxels);
-/* One round; *running and *queued receive the counts afterwards. */
+/* Cancel request id (queued or running): it leaves the queue or the batch,
+ * its device memory is freed, its status becomes VOCE_REQ_CANCELLED (error
+ * VOCE_ERR_CANCELLED) and t_done the cancellation time.  VOCE_ERR_STATE if it
+ * has already ended. */
+int voce_server_cancel(voce_server *s, long long id);
+/* Deadline of request id: server time t (voce_server_now's clock; 0 clears
+ * it).  A request not done when a voce_server_poll starts at or after t is
+ * ended there: status VOCE_REQ_FAILED, error VOCE_ERR_DEADLINE, its device
+ * memory freed.  VOCE_ERR_STATE if it has already ended. */
+int voce_server_set_deadline(voce_server *s, long long id, double t);
+/* One round; *running and *queued receive the counts afterwards.  Expired
+ * deadlines are handled first, then admission, then the batch ticks. */
 int voce_server_poll(voce_server *s, int *running, int *queued);
 double voce_server_now(const voce_server *s);
 int voce_server_info(const voce_server *s, long long id, voce_request_info *out);

@@ -91,7 +91,7 @@ def test_footprint_scales_with_grid(voce_lib):
     # (the FP64 form also stores n and omega of every frequency: 9 doubles)
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec - 9 * 8 * nspec
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 840 * nv - 2 * 9 * 8 * nspec
-    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_IR) == a + 420 * nv - 2 * 9 * 8 * nspec
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_IR) == a + 840 * nv - 2 * 9 * 8 * nspec
     assert capi.footprint((256, 256, 256)) < 40e9
 
 
@@ -164,3 +164,45 @@ def test_fft_schedule_candidates(voce_lib):
             256: 1, 384: 4, 5: 0, 10: 0, 1: 0}
     for n, c in want.items():
         assert lib.voce_fft_schedule_count(n) == c, n
+
+
+def test_server_cancel_and_deadline_on_the_host(voce_lib):
+    """Queue handling of voce_serve.h without a GPU: a server that has
+    admitted nothing needs no device.  A queued request is cancelled (status
+    CANCELLED, error ERR_CANCELLED, t_done set); one whose deadline has
+    passed ends at the start of the next poll with ERR_DEADLINE, before any
+    admission; ended requests cannot be cancelled or given a deadline again.
+    A budget smaller than every footprint keeps the remaining request from
+    being admitted, so that no GPU work is tried."""
+    from voce_gb300 import synth
+    c = synth.small_case(8, 3, 5, n_steps=1)
+    d = tempfile.mkdtemp(prefix="srv_host_")
+    nlp = c.write(d)
+    nl = capi.read_namelist(nlp)
+    sx = capi.read_slip(os.path.join(d, "mat.sx"))
+    tiny = capi.footprint((8, 8, 8)) // 2
+    with capi.Server(capi.PREC_MIXED_IR, tiny, ticks_per_round=2) as s:
+        args = (nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, 1)
+        a, b, late = s.submit(*args), s.submit(*args), s.submit(*args)
+        s.cancel(b)
+        ib = s.info(b)
+        assert ib.status == capi.REQ_CANCELLED and ib.error == capi.ERR_CANCELLED
+        assert ib.t_done >= ib.t_submit
+        s.set_deadline(late, 1e-9)                     # already past
+        assert s.info(late).t_deadline > 0
+        with pytest.raises(capi.VoceError) as e:
+            s.cancel(b)
+        assert e.value.code == 9
+        run, que = s.poll()
+        il = s.info(late)
+        assert il.status == capi.REQ_FAILED and il.error == capi.ERR_DEADLINE
+        # a's footprint exceeds the budget: it fails with ERR_NOMEM, no device work
+        ia = s.info(a)
+        assert ia.status == capi.REQ_FAILED and ia.error == 7
+        assert (run, que) == (0, 0) and s.bytes_in_use == 0
+        for rid in (a, late):
+            with pytest.raises(capi.VoceError):
+                s.set_deadline(rid, s.now() + 5.0)
+        with pytest.raises(capi.VoceError) as e:
+            s.cancel(12345)
+        assert e.value.code == 1

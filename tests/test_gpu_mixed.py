@@ -119,13 +119,18 @@ def test_mixed_chord_steps_against_exact_jacobian(name, voce_lib):
     assert gio.rel(chord[2], exact[2]) < 1e-6
 
 
+@pytest.mark.parametrize("pred", [0, 1])
 @pytest.mark.parametrize("name", ["vor8_psc", "vor12_mix", "cfg1_16"])
-def test_float_jacobian_converges_to_the_fp64_residual_root(name, voce_lib):
-    """VOCE_PREC_MIXED_IR against VOCE_PREC_MIXED with the exact FP64
-    Jacobian (chord steps off): both drive the same FP64 residual to its root
-    under the same stop test, so they differ only by where each stops
-    (updates below 1e-7 relative) -- macro averages within 1e-7, fields
-    within 1e-6, Green-iteration counts within one."""
+def test_float_jacobian_converges_to_the_fp64_residual_root(name, pred, voce_lib):
+    """VOCE_PREC_MIXED_IR (with and without its FP32-pipe start) against
+    VOCE_PREC_MIXED with the exact FP64 Jacobian (chord steps off): both drive
+    the same FP64 residual to its root under the same stop test, so they
+    differ only by where each stops (updates below 1e-7 relative): macro
+    averages within 1e-7, stress fields within 1e-6, Green-iteration counts
+    within one.  The strain rate is evaluated at the stress before the last
+    Newton update (evolution.c:67), which lies up to the stop tolerance from
+    the root; through the n = 20 power law that moves it by up to ~2e-6, so
+    strain-rate fields are held to 1e-5."""
     make, n, _ = make_golden.CASES[name]
     case = make()
     nl = _write(case)
@@ -137,11 +142,15 @@ def test_float_jacobian_converges_to_the_fp64_residual_root(name, voce_lib):
             exact = ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"))
     finally:
         lib.voce_set_newton_chord(1)
-    with capi.Rve.from_files(nl, capi.PREC_MIXED_IR) as r:
-        r.run(n)
-        ir = ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"))
+    lib.voce_set_ir_predictor(pred)
+    try:
+        with capi.Rve.from_files(nl, capi.PREC_MIXED_IR) as r:
+            r.run(n)
+            ir = ([r.increment(k) for k in range(n)], r.field("sig_voigt"), r.field("edot_voigt"))
+    finally:
+        lib.voce_set_ir_predictor(1)
     for a, b in zip(ir[0], exact[0]):
         assert abs(a["iters"] - b["iters"]) <= 1
         assert gio.rel(a["sig_avg"], b["sig_avg"]) < 1e-7
     assert gio.rel(ir[1], exact[1]) < 1e-6
-    assert gio.rel(ir[2], exact[2]) < 1e-6
+    assert gio.rel(ir[2], exact[2]) < 1e-5

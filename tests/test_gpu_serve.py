@@ -137,3 +137,59 @@ def test_active_limit_keeps_voxels_in_flight_under_it(voce_lib):
         for rid, c, sig in zip(ids, cases, alone):
             assert s.info(rid).status == capi.REQ_DONE
             assert np.array_equal(s.result(rid, "sig_voigt", c.mesh.nvox), sig)
+
+
+def test_cancel_and_deadline_leave_the_others_bit_identical(voce_lib):
+    """Four requests in one running batch: one is cancelled while it runs,
+    one is given a deadline that expires mid-run, one is cancelled while
+    still queued behind the active limit.  Each ended request frees its
+    device memory at once; the survivors finish with the same bits as the
+    same RVEs solved alone."""
+    rng = np.random.Generator(np.random.PCG64(78))
+    cases = []
+    for i, (n, g, inc) in enumerate([(16, 10, 3), (12, 6, 3), (16, 12, 3), (8, 4, 2), (12, 5, 2)]):
+        c = synth.small_case(n, g, 600 + i, n_steps=inc, load=synth.random_traceless_load(rng))
+        c.iter_max = 40
+        cases.append((c, inc))
+    keep = [0, 3]
+    alone = {}
+    for k in keep:
+        c, n = cases[k]
+        nlp, _, _ = _inputs(c)
+        with capi.Rve.from_files(nlp) as r:
+            r.run(n)
+            alone[k] = (r.increment(n - 1), r.field("sig_voigt"), r.field("edot_voigt"))
+    with capi.Server(capi.PREC_FP64, 64 << 30, ticks_per_round=3, keep_fields=True) as s:
+        # room for the first four in flight, the fifth waits in the queue
+        s.set_active_limit(sum(c.mesh.nvox for c, _ in cases[:4]))
+        ids = []
+        for c, n in cases:
+            _, nl, sx = _inputs(c)
+            ids.append(s.submit(nl, sx, c.mesh.euler_deg, c.mesh.grain, c.mesh.phase, n))
+        run, que = s.poll()
+        assert (run, que) == (4, 1)
+        used = s.bytes_in_use
+        s.cancel(ids[1])                                   # running
+        assert s.info(ids[1]).status == capi.REQ_CANCELLED
+        assert s.bytes_in_use == used - capi.footprint(cases[1][0].mesh.dims)
+        s.cancel(ids[4])                                   # queued
+        s.set_deadline(ids[2], s.now() + 0.05)             # running, expires soon
+        import time
+        time.sleep(0.1)
+        for _ in range(100000):
+            run, que = s.poll()
+            if run == 0 and que == 0:
+                break
+        i2 = s.info(ids[2])
+        assert i2.status == capi.REQ_FAILED and i2.error == capi.ERR_DEADLINE
+        assert i2.increments_done < cases[2][1]
+        assert s.info(ids[4]).status == capi.REQ_CANCELLED and s.info(ids[4]).t_admit == 0.0
+        assert s.bytes_in_use == 0
+        for k in keep:
+            c, n = cases[k]
+            info = s.info(ids[k])
+            inc, sig, edot = alone[k]
+            assert info.status == capi.REQ_DONE and info.increments_done == n
+            assert info.last.iters == inc["iters"] and list(info.last.sig_avg) == inc["sig_avg"]
+            assert np.array_equal(s.result(ids[k], "sig_voigt", c.mesh.nvox), sig)
+            assert np.array_equal(s.result(ids[k], "edot_voigt", c.mesh.nvox), edot)

@@ -20,7 +20,7 @@ LEGACY_LIB_PATH = os.path.join(HERE, "lib", "libvoce_legacy.so")
 VOCE_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_PARSE", 4: "ERR_BC",
           5: "ERR_SINGULAR", 6: "ERR_UNSUPPORTED", 7: "ERR_NOMEM", 8: "ERR_CUDA",
-          9: "ERR_STATE"}
+          9: "ERR_STATE", 10: "ERR_CANCELLED", 11: "ERR_DEADLINE"}
 PREC_FP64, PREC_MIXED, PREC_MIXED_NR32, PREC_MIXED_IR = 0, 1, 2, 3
 NOALLOC_MAX_DOUBLES = 4194304   # VOCE_NOALLOC_MAX_DOUBLES
 # .iout dump kinds (include/voce_io.h)
@@ -162,10 +162,13 @@ PROTOTYPES = [
     ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_fft_schedule_count", C.c_int, [C.c_int]),
     ("voce_set_newton_chord", C.c_int, [C.c_int]),
+    ("voce_set_ir_predictor", C.c_int, [C.c_int]),
     ("voce_rve_get_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]),
     ("voce_rve_set_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("voce_server_set_quantum", C.c_int, [C.c_void_p, C.c_int]),
     ("voce_server_set_active_limit", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("voce_server_cancel", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("voce_server_set_deadline", C.c_int, [C.c_void_p, C.c_longlong, C.c_double]),
 ]
 KERNELS = ["fft_z_fwd", "fft_y_fwd", "fft_x_green", "fft_y_inv", "fft_z_inv", "nr",
            "finalize_iter", "prelude", "incr_fft", "incr_end", "finalize_incr"]
@@ -553,10 +556,11 @@ class RequestInfo(C.Structure):
                 ("increments_done", C.c_int), ("increments_wanted", C.c_int),
                 ("dims", C.c_int * 3), ("t_submit", C.c_double), ("t_admit", C.c_double),
                 ("t_done", C.c_double), ("voxel_iterations", C.c_longlong),
-                ("last", VoceIncrement), ("preemptions", C.c_int)]
+                ("last", VoceIncrement), ("preemptions", C.c_int), ("t_deadline", C.c_double)]
 
 
-REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
+ERR_CANCELLED, ERR_DEADLINE = 10, 11
 
 
 class Server:
@@ -593,6 +597,15 @@ class Server:
         """Admit only while the admitted requests hold at most this many
         voxels (0: no limit)."""
         _check(load().voce_server_set_active_limit(self._h, int(voxels)))
+
+    def cancel(self, rid: int) -> None:
+        """End a queued or running request; its device memory is freed."""
+        _check(load().voce_server_cancel(self._h, rid))
+
+    def set_deadline(self, rid: int, t: float) -> None:
+        """Server time (now()'s clock) by which the request must be done;
+        0 clears it."""
+        _check(load().voce_server_set_deadline(self._h, rid, float(t)))
 
     def poll(self):
         run = C.c_int()

@@ -419,6 +419,7 @@ namespace {
 int autotune_tiles(voce_rve *r);
 extern int g_autotune;
 extern int g_newton_chord;
+extern int g_ir_predictor;
 
 // Device arrays of one RVE, state and scratch, sized from its descriptor;
 // the twiddle tables are filled, the rest is left to the caller.
@@ -438,8 +439,6 @@ int alloc_device(voce_rve *r)
     d.sch_lo = d.itau_lo = d.sgp_lo = nullptr;
     if (d.nr32 || d.ir) {
         AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv);
-    }
-    if (d.nr32) {
         AL(d.sch_lo, 60 * nv); AL(d.itau_lo, 24 * nv); AL(d.sgp_lo, 21 * nv);
     }
     AL(d.part, (size_t)3 * r->npart * VOCE_NPART);
@@ -491,8 +490,6 @@ void for_state(RveDesc &d, F &&f)
         f((void **)&d.sch32, 60 * nv * S);
         f((void **)&d.itau32, 24 * nv * S);
         f((void **)&d.sgp32, 21 * nv * S);
-    }
-    if (d.nr32) {
         f((void **)&d.sch_lo, 60 * nv * S);
         f((void **)&d.itau_lo, 24 * nv * S);
         f((void **)&d.sgp_lo, 21 * nv * S);
@@ -516,9 +513,9 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // sg 21, crss 24, itau 24, gamacum 1, gtot 12, edot 5, gamdot 12, taux 12,
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
     // + the FP64 form's stored Green-operator frequencies, 9 doubles each
-    // + the mixed_nr32 form's float pairs of sch, itau and S_g + S0 (2 x 105
-    // floats), the mixed_ir form's float copies of the same (105 floats)
-    const long long f32 = precision == VOCE_PREC_MIXED_NR32 ? 840 : precision == VOCE_PREC_MIXED_IR ? 420 : 0;
+    // + the mixed_nr32 and mixed_ir forms' float pairs of sch, itau and
+    // S_g + S0 (2 x 105 floats)
+    const long long f32 = (precision == VOCE_PREC_MIXED_NR32 || precision == VOCE_PREC_MIXED_IR) ? 840 : 0;
     return nv * (214 * 8 + 4 + f32) + nspec * 9 * cplx +
            (precision == VOCE_PREC_FP64 ? nspec * 9 * 8 : 0);
 }
@@ -585,6 +582,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     d.chord = r->precision == VOCE_PREC_MIXED ? g_newton_chord : 0;
     d.nr32 = r->precision == VOCE_PREC_MIXED_NR32;
     d.ir = r->precision == VOCE_PREC_MIXED_IR;
+    d.ir_pred = d.ir ? g_ir_predictor : 0;
     for (int p = 0; p < 2; ++p) d.solid[p + 1] = (p < nl->N_phases && !nl->Type_phases[p]) ? 1 : 0;
     d.nsys = sx.nsys;
     d.update_flag = nl->Update_Flag;
@@ -927,6 +925,7 @@ std::mutex g_tile_mu;
 std::map<TileKey, Tiles> g_tile_cache;
 int g_autotune = 1;
 int g_newton_chord = 1;   // chord steps in the FP64 Newton of new VOCE_PREC_MIXED RVEs
+int g_ir_predictor = 1;   // single-precision start of the FP64 steps in new VOCE_PREC_MIXED_IR RVEs
 
 // schedule index k of an axis of length L (the default when out of range)
 FftPlan1 schedule_of(int L, int k)
@@ -1691,6 +1690,12 @@ int voce_rve_get_tiles(const voce_rve *r, int tiles[6])
 int voce_set_newton_chord(int on)
 {
     g_newton_chord = on ? 1 : 0;
+    return VOCE_OK;
+}
+
+int voce_set_ir_predictor(int on)
+{
+    g_ir_predictor = on ? 1 : 0;
     return VOCE_OK;
 }
 

@@ -88,6 +88,7 @@ struct RveDesc {
     int chord;           // FP64 Newton: reuse the last Jacobian once the update is below 1e-4
     int nr32;            // Newton iterations in float with an FP64 acceptance step
     int ir;              // Newton on the FP64 residual with a float Jacobian and solve
+    int ir_pred;         // ir: the FP64 steps start from a single-precision / float-float solve
     double dt, wgt, wgt_ph1, err_tol, inv_nv;
     double wgt_ratio;    // wgt / wgt_ph1 (the same IEEE division, once on the host)
     int all_ph1;         // every voxel is phase 1 (the phase-1 sums equal the full ones)
@@ -121,7 +122,6 @@ struct RveDesc {
     float *itau32;       // float copy of itau (float-Jacobian Newton forms only)
     float *sgp32;        // float (S_g + S0), packed upper triangle (float-Jacobian Newton forms only)
     float *sch_lo, *itau_lo, *sgp_lo;   // x - (double)x32 rounded to float, for the same three
-                                        // (the FP32-Newton form only; null otherwise)
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;

@@ -255,6 +255,37 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
 // ---------------------------------------------------------------------------
 // FFT passes
 // ---------------------------------------------------------------------------
+// Tile copy of n elements by the block: each thread first loads U elements
+// (i, i + nthr, ...) into registers, then stores them, so that U global loads
+// per thread are in flight at once instead of one load-store pair at a time.
+// ld(i) returns element i, st(i, value) places it.
+template <int U, typename T, class LD, class ST>
+__device__ __forceinline__ void staged_copy(int n, LD ld, ST st)
+{
+    const int nt = blockDim.x;
+    for (int b = threadIdx.x; b < n; b += U * nt) {
+        T v[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+            const int i = b + j * nt;
+            if (i < n) v[j] = ld(i);
+        }
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+            const int i = b + j * nt;
+            if (i < n) st(i, v[j]);
+        }
+    }
+}
+// loads in flight per thread: the single-precision passes wait on memory, the
+// double-precision ones on the FP64 pipe (there one at a time, as before,
+// keeps their registers and occupancy)
+template <typename R> struct CopyDepth { static constexpr int v = 8; };
+template <> struct CopyDepth<double> { static constexpr int v = 1; };
+// the z passes gather strided columns and convert: measured slower with
+// deeper copies (more registers, fewer resident blocks), so one at a time
+constexpr int kZCopyDepth = 1;
+
 // the stress's six components into the spectrum (evolution.c:350-361)
 template <typename R>
 __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
@@ -269,12 +300,15 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
     const int ytiles = ny / rows;
     const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const long long vb = ((long long)x * ny + y0) * nz;
-    for (int idx = threadIdx.x; idx < 6 * rows * nz; idx += blockDim.x) {
-        const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
-        const R val = (R)__ldg(d.sig + c * nv + vb + (long long)r * nz + z);
-        C *e = &bufA[z * ldl + (c >> 1) * rows + r];
-        if (c & 1) e->y = val; else e->x = val;
-    }
+    // element idx = (c * rows + r) * nz + z is sig[c][vb + r * nz + z]
+    staged_copy<kZCopyDepth, double>(
+        6 * rows * nz,
+        [&](int idx) { return __ldg(d.sig + (idx / (rows * nz)) * nv + vb + idx % (rows * nz)); },
+        [&](int idx, double v) {
+            const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+            C *e = &bufA[z * ldl + (c >> 1) * rows + r];
+            if (c & 1) e->y = (R)v; else e->x = (R)v;
+        });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, -1);
     C *spec = (C *)d.spec;
@@ -353,10 +387,9 @@ __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int 
     const int x0 = (unit % xtiles) * xt;
     C *spec = (C *)specp;
     const long long base = ((long long)line * nx + x0) * ny;
-    for (int idx = threadIdx.x; idx < xt * ny; idx += blockDim.x) {
-        const int xl = idx / ny, y = idx % ny;
-        bufA[y * ldl + xl] = spec[base + idx];
-    }
+    staged_copy<CopyDepth<R>::v, C>(
+        xt * ny, [&](int idx) { return spec[base + idx]; },
+        [&](int idx, C v) { bufA[(idx % ny) * ldl + idx / ny] = v; });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.ply, (const C *)d.twy, sign);
     for (int idx = threadIdx.x; idx < xt * ny; idx += blockDim.x) {
@@ -381,10 +414,16 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     C *aacc = (C *)d.aacc;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
-    for (int idx = threadIdx.x; idx < 6 * nx * kc; idx += blockDim.x) {
-        const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-        bufA[x * ldl + c * kc + yl] = spec[c * cstride + kb + (long long)x * ny + yl];
-    }
+    staged_copy<CopyDepth<R>::v, C>(
+        6 * nx * kc,
+        [&](int idx) {
+            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+            return spec[c * cstride + kb + (long long)x * ny + yl];
+        },
+        [&](int idx, C v) {
+            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+            bufA[x * ldl + c * kc + yl] = v;
+        });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, -1);
     C *oth = (res == bufA) ? bufB : bufA;
@@ -442,10 +481,16 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
     C *spec = (C *)specp;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
-    for (int idx = threadIdx.x; idx < ncomp * nx * kc; idx += blockDim.x) {
-        const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-        bufA[x * ldl + c * kc + yl] = spec[c * cstride + kb + (long long)x * ny + yl];
-    }
+    staged_copy<CopyDepth<R>::v, C>(
+        ncomp * nx * kc,
+        [&](int idx) {
+            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+            return spec[c * cstride + kb + (long long)x * ny + yl];
+        },
+        [&](int idx, C v) {
+            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+            bufA[x * ldl + c * kc + yl] = v;
+        });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, sign);
     for (int idx = threadIdx.x; idx < ncomp * nx * kc; idx += blockDim.x) {
@@ -477,35 +522,47 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long xy = (long long)x * ny + y0;
     const int half = nz / 2;
-    for (int idx = threadIdx.x; idx < np * nz * rows; idx += blockDim.x) {
-        const int r = idx % rows, t = idx / rows, k = t % nz, p = t / nz;
-        const int ca = 2 * p, cb = 2 * p + 1;
-        const bool lo = k <= half;
-        const int ks = lo ? k : nz - k;
-        const long long o = (long long)ks * plane + xy + r;
-        C A = spec[ca * cstride + o], B;
-        if (cb < ncomp) B = spec[cb * cstride + o];
-        else { B.x = R(0); B.y = R(0); }
-        if (k == 0 || k == half) { A.y = R(0); B.y = R(0); }
-        if (!lo) { A.y = -A.y; B.y = -B.y; }
-        C Z;
-        Z.x = A.x - B.y;
-        Z.y = A.y + B.x;
-        bufA[k * ldl + p * rows + r] = Z;
-    }
+    struct AB { C a, b; };
+    staged_copy<kZCopyDepth, AB>(
+        np * nz * rows,
+        [&](int idx) {
+            const int r = idx % rows, t = idx / rows, k = t % nz, p = t / nz;
+            const int ca = 2 * p, cb = 2 * p + 1;
+            const int ks = k <= half ? k : nz - k;
+            const long long o = (long long)ks * plane + xy + r;
+            AB v;
+            v.a = spec[ca * cstride + o];
+            if (cb < ncomp) v.b = spec[cb * cstride + o];
+            else { v.b.x = R(0); v.b.y = R(0); }
+            return v;
+        },
+        [&](int idx, AB v) {
+            const int r = idx % rows, t = idx / rows, k = t % nz, p = t / nz;
+            const bool lo = k <= half;
+            C A = v.a, B = v.b;
+            if (k == 0 || k == half) { A.y = R(0); B.y = R(0); }
+            if (!lo) { A.y = -A.y; B.y = -B.y; }
+            C Z;
+            Z.x = A.x - B.y;
+            Z.y = A.y + B.x;
+            bufA[k * ldl + p * rows + r] = Z;
+        });
     __syncthreads();
     const C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, +1);
     const long long vb = xy * nz;
     const double inv = d.inv_nv;
     if (mode == 0) {
         const MacroDev *m = d.macro;
-        for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x) {
-            const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
-            const C e = res[z * ldl + (c >> 1) * rows + r];
-            const double val = (double)((c & 1) ? e.y : e.x);
-            const long long g = (long long)c * nv + vb + (long long)r * nz + z;
-            d.dgs[g] += m->ddg6[c] + val * inv;
-        }
+        // element idx = (c * rows + r) * nz + z is dgs[c][vb + r * nz + z]
+        staged_copy<kZCopyDepth, double>(
+            ncomp * rows * nz,
+            [&](int idx) { return d.dgs[(idx / (rows * nz)) * nv + vb + idx % (rows * nz)]; },
+            [&](int idx, double old) {
+                const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+                const C e = res[z * ldl + (c >> 1) * rows + r];
+                const double val = (double)((c & 1) ? e.y : e.x);
+                d.dgs[(long long)c * nv + vb + (long long)r * nz + z] = old + (m->ddg6[c] + val * inv);
+            });
     } else if (mode == 1) {
         for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x) {
             const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
@@ -803,6 +860,94 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
 // shear ratio |r| >= 60 (where |r|^(n-1) could leave the float range) makes
 // that iteration take the FP64 Jacobian instead.  gam0 is one value for all
 // systems (one slip mode), so it is applied once to the strain-rate sums.
+//
+// With d.ir_pred the FP64 iterations start from a point computed on the FP32
+// pipe (ir_start): single-precision Newton steps down to a relative update of
+// 1e-4, then one step on the float-float residual (residual_ff, the model
+// data as float pairs, about 48 bits) with the last single-precision matrix.
+// That point lies within about 1e-9 relative of the FP64 residual's root, so
+// the first FP64 step's update is already below the 1e-7 stop test: one FP64
+// residual evaluation per voxel accepts it, against two to seven from the
+// Green iterate.  The start never decides the result -- the accepted stress
+// and the stop decision come from the FP64 steps.  A start that does not
+// converge in single precision, meets a resolved-shear ratio too large for
+// |r|^n in FP32 or a non-finite value is dropped (the FP64 steps then start
+// from the Green iterate).  st is the voxel's staged column of float Schmid
+// vectors and 1/CRSS (as in the single-precision Newton form).
+__device__ __forceinline__ bool ir_start(const RveDesc &d, long long v, const float *st,
+                                         const double (&lam)[6], const double (&cc)[6], double sn2,
+                                         double (&sig)[6], int &it)
+{
+    float sf[6], ccf[6], Pf[21], Mf[6][6];
+#pragma unroll
+    for (int q = 0; q < 21; ++q) Pf[q] = __ldg(d.sgp32 + (long long)q * d.nv + v);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) { sf[c] = (float)lam[c]; ccf[c] = (float)cc[c]; }
+    // single precision stops at a relative update of 1e-4 (its rounding
+    // floor can lie near 1e-5); the float-float step then takes the point to
+    // within Newton's quadratic term of that update (~1e-9)
+    const float thr32 = (float)(1e-8 * sn2);
+    const float dtf = d.dth;
+    bool conv = false;
+    cp_async_wait_all();   // the staged column of this voxel
+    for (int p = 0; p < 12; ++p) {
+        float ed[5], D[15], x[6];
+        if (!flow_rule_f32(d, st, sf, ed, D)) return false;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            float t = ccf[i] + (i < 5 ? dtf * ed[i] : 0.0f);
+#pragma unroll
+            for (int j = 0; j < 6; ++j) t = fmaf(Pf[sym6(i, j)], sf[j], t);
+            x[i] = t;
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+                float m = Pf[sym6(i, j)];
+                if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                Mf[i][j] = m;
+            }
+        }
+        ldlt_solve6f(Mf, x);
+        float dn = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) { dn = fmaf(x[c], x[c], dn); sf[c] -= x[c]; }
+        ++it;
+        if (!(dn <= 3.0e38f)) return false;   // not finite
+        if (dn < thr32) { conv = true; break; }
+    }
+    if (!conv) return false;
+    float x[6];
+    if (!residual_ff(d, v, st, sf, cc, Pf, x)) return false;
+    ldlt_solve6f(Mf, x);
+    ++it;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c] - (double)x[c];
+    return true;
+}
+
+// One FP64-Jacobian step of newton_ir, for the rare iteration whose
+// resolved-shear ratio leaves the float range; kept out of line so that its
+// registers do not weigh on the common path.
+__device__ __noinline__ void ir_fp64_step(const RveDesc &d, long long v, const double *P, const double *sig,
+                                          double *R)
+{
+    double Dd[15], edd[5];
+    flow_rule<true, false, double>(d, v, sig, edd, Dd, nullptr, nullptr);
+    double M[6][6], b[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        b[i] = R[i];
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+            double m = P[sym6(i, j)];
+            if (i < 5 && j < 5) m = fma(d.dt, Dd[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+            M[i][j] = m;
+        }
+    }
+    ldlt_solve6(M, b);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) R[i] = b[i];
+}
+
 __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const double (&P)[21],
                                           const double (&cc)[6], double thr, double (&sig)[6],
                                           double (&sp)[6], double (&Rl)[6], int &it)
@@ -875,18 +1020,7 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
 #pragma unroll
             for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
         } else {
-            double Dd[15], edd[5];
-            flow_rule<true, false, double>(d, v, sig, edd, Dd, nullptr, nullptr);
-            double M[6][6];
-#pragma unroll
-            for (int i = 0; i < 6; ++i)
-#pragma unroll
-                for (int j = 0; j <= i; ++j) {
-                    double m = P[sym6(i, j)];
-                    if (i < 5 && j < 5) m = fma(d.dt, Dd[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
-                    M[i][j] = m;
-                }
-            ldlt_solve6(M, R);
+            ir_fp64_step(d, v, P, sig, R);
         }
         double cnr = 0.0;
 #pragma unroll
@@ -926,7 +1060,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
     const long long nv = d.nv;
     for (long long v = (long long)unit * blockDim.x + threadIdx.x; v < nv;
          v += (long long)nunits * blockDim.x) {
-        if (NR32) {
+        if (NR32 || IR) {
             // asynchronous copies of the voxel's float Schmid vectors and
             // 1/CRSS; every path below waits for them before the next voxel
 #pragma unroll
@@ -939,7 +1073,7 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
         if (!d.solid[ph]) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = 0.0; d.sigp[c * nv + v] = 0.0; }
-            if (NR32) cp_async_wait_all();
+            if (NR32 || IR) cp_async_wait_all();
             continue;
         }
         double lam[6], cc[6];
@@ -975,8 +1109,20 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             double P[21];
             load_P(d, v, P);
             // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
-            if (IR && d.ipow_n >= 1) newton_ir(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
-            else newton_fp64<IR, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            if (IR && d.ipow_n >= 1) {
+                if (d.ir_pred) {
+                    int it0 = it;
+                    if (!ir_start(d, v, st, lam, cc, sn2, sig, it)) {
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) sig[c] = lam[c];
+                        it = it0;
+                    }
+                }
+                newton_ir(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            } else {
+                newton_fp64<IR, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
+            }
+            if (IR) cp_async_wait_all();
         }
         double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
         if (NR32) {
@@ -1075,114 +1221,145 @@ __device__ double svm_of(const double *t9)
     return sqrt(3. / 2. * s);
 }
 
-// one thread: errors, volume averages, mixed-BC macro correction,
-// convergence decision (evolution.c:401-431, get_smacro :170-241)
+// Errors, volume averages, mixed-BC macro correction and the convergence
+// decision (evolution.c:401-431, get_smacro :170-241), after the block's
+// reduction of the partial sums, by the block's first warp.  Every value is
+// computed by one lane with the operations, in the order, a single thread
+// would use, so the results do not depend on the split; the lanes compute
+// independent values side by side (the 9 + 9 stress averages, the 6 mixed-BC
+// corrections, the two von Mises norms, the two error normalisations, the
+// epilogue's 9 velocity-gradient divisions and its two norms), each step as
+// one instruction stream for the warp.  That cuts the dependent chain of
+// slow FP64 operations (~60-cycle DADD/DFMA latency, ~1500-cycle divisions)
+// that bounds this kernel.  m is the block's shared-memory copy.
 __device__ void finalize_iter_body(const RveDesc &d, MacroDev *m, int npart)
 {
     double tot[VOCE_NPART];
     reduce_partials(d.part, npart, tot);
-    if (threadIdx.x != 0) return;
-    static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
-    // the macro inputs, loaded together; the updates are computed in
-    // registers and stored once (same operations, same order)
+    const int lane = threadIdx.x;
+    if (lane >= 32) return;
+    __shared__ double s_dg[9], s_vm2[2], s_act[2][9];
+    const int IJV0[6] = {0, 1, 2, 1, 0, 0}, IJV1[6] = {0, 1, 2, 2, 2, 1};
     const int first_iter = m->first_iter, it = m->iter, istep = m->istep;
     const double Err_e0 = m->Err_e, Err_s0 = m->Err_s, e_vm = m->e_vm;
-    double dg[9], acum[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        dg[q] = m->dDisGradAvg[q];   // entries get_smacro leaves alone keep their value
-        acum[q] = m->dDisGradAvg_acum[q];
-    }
     // the mixed form's Newton ran in single precision alone this iteration
     // (the predicate nr_unit used): it may not end the increment
     const bool fp32_only = d.nr32 && (first_iter || fmax(fabs(Err_e0), fabs(Err_s0)) > VOCE_POLISH_ERR);
-    double Err_e = tot[1] * d.wgt, Err_s = tot[0] * d.wgt;
-    double s9[9], s19[9], sa[9], sa1[9];
-    sym9_from_b(tot + 2, s9);
-    sym9_from_b(tot + 8, s19);
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        sa[q] = s9[q] * d.wgt;
-        sa1[q] = s19[q] * d.wgt_ratio;
-        m->SigAvg[q] = sa[q];
-        m->SigAvg1[q] = sa1[q];
+    // lane q < 9: SigAvg[q]; lane 9 + q: SigAvg1[q] (phase 1)
+    if (lane < 18) {
+        double s9[9];
+        sym9_from_b(tot + (lane < 9 ? 2 : 8), s9);
+        const int q = lane < 9 ? lane : lane - 9;
+        const double v = s9[q] * (lane < 9 ? d.wgt : d.wgt_ratio);
+        if (lane < 9) m->SigAvg[q] = v;
+        else m->SigAvg1[q] = v;
     }
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const int ii = IJV[0][i], jj = IJV[1][i];
+    // entries get_smacro leaves alone keep their value
+    if (lane < 9) s_dg[lane] = m->dDisGradAvg[lane];
+    __syncwarp();
+    // lane i < 6: dDisGradAvg at IJV(i) (get_smacro)
+    if (lane < 6) {
+        const int ii = IJV0[lane], jj = IJV1[lane];
         double s = 0.0;
-        if (d.vflag[i] == 0)
+        if (d.vflag[lane] == 0)
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
-                const int kk = IJV[0][k], ll = IJV[1][k];
+                const int kk = IJV0[k], ll = IJV1[k];
                 s += d.S0t[((ii * 3 + jj) * 3 + kk) * 3 + ll] * d.sflag[k] *
-                     (d.Scauchy[kk * 3 + ll] - sa[kk * 3 + ll]);
+                     (d.Scauchy[kk * 3 + ll] - m->SigAvg[kk * 3 + ll]);
             }
-        dg[ii * 3 + jj] = s;
+        s_dg[ii * 3 + jj] = s;
     }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        acum[q] += dg[q];
-        m->dDisGradAvg[q] = dg[q];
-        m->dDisGradAvg_acum[q] = acum[q];
+    __syncwarp();
+    if (lane < 9) {
+        const double dg = s_dg[lane];
+        m->dDisGradAvg[lane] = dg;
+        m->dDisGradAvg_acum[lane] += dg;
     }
-    const double svm = svm_of(sa), svm1 = svm_of(sa1);
-    m->s_vm = svm;
-    m->s_vm1 = svm1;
-    if (fabs(e_vm) > 1E-5) Err_e /= e_vm;
-    Err_s /= svm;
-    m->Err_e = Err_e;
-    m->Err_s = Err_s;
-    if (it < d.iter_max) {
+    // lane 0: s_vm, lane 1: s_vm1
+    if (lane < 2) {
+        const double v = svm_of(lane == 0 ? m->SigAvg : m->SigAvg1);
+        if (lane == 0) m->s_vm = v;
+        else m->s_vm1 = v;
+        s_vm2[lane] = v;
+    }
+    __syncwarp();
+    // lane 0: Err_s = sum / s_vm; lane 1: Err_e = sum / e_vm when e_vm > 1e-5
+    // (x / 1.0 is x exactly, so the untaken division is a division by one)
+    double err = 0.0;
+    if (lane < 2) {
+        const double num = tot[lane == 0 ? 0 : 1] * d.wgt;
+        const double den = lane == 0 ? s_vm2[0] : (fabs(e_vm) > 1E-5 ? e_vm : 1.0);
+        err = num / den;
+    }
+    const double Err_s = __shfl_sync(0xffffffffu, err, 0), Err_e = __shfl_sync(0xffffffffu, err, 1);
+    if (lane == 0) {
+        m->Err_e = Err_e;
+        m->Err_s = Err_s;
+    }
+    if (it < d.iter_max && lane < VOCE_ITLOG) {
         const int slot = (istep - 1) % d.incr_cap;
         double *lg = d.itlog + ((long long)slot * d.iter_max + it) * VOCE_ITLOG;
-        lg[0] = Err_e;
-        lg[1] = Err_s;
-        lg[2] = svm;
-        lg[3] = tot[14];
-        lg[4] = tot[1];   // raw sum of the strain-compatibility norms
-        lg[5] = tot[0];   // raw sum of the stress-change norms
-        for (int q = 0; q < 6; ++q) lg[6 + q] = tot[2 + q];  // sum of sigma (basis)
+        double v;
+        switch (lane) {
+        case 0: v = Err_e; break;
+        case 1: v = Err_s; break;
+        case 2: v = s_vm2[0]; break;
+        case 3: v = tot[14]; break;
+        case 4: v = tot[1]; break;   // raw sum of the strain-compatibility norms
+        case 5: v = tot[0]; break;   // raw sum of the stress-change norms
+        default: v = tot[2 + lane - 6]; break;   // sum of sigma (basis)
+        }
+        lg[lane] = v;
     }
-    m->iter = it + 1;
-    m->iter_total += 1;
-    m->nr_total += tot[14];
-    m->nr_max = max(m->nr_max, (int)tot[15]);
-    double t6[6] = {dg[0], dg[4], dg[8], 0.5 * (dg[5] + dg[7]), 0.5 * (dg[2] + dg[6]), 0.5 * (dg[1] + dg[3])};
-    t6_to_b<double>(t6, m->ddg6);
-    m->first_iter = 0;
-    m->pending_prelude = 0;
+    __syncwarp();
     const bool more = (it + 1 < d.iter_max) &&
                       (fp32_only || fmax(fabs(Err_s), fabs(Err_e)) > fabs(d.err_tol));
-    m->converged = more ? 0 : 1;
-    if (!more) {
-        // epilogue macro bookkeeping (evolution.c:438-461)
-        double act[9], vga[9];
-        for (int q = 0; q < 9; ++q) {
-            act[q] = m->DisGradAvg[q] + acum[q];
-            vga[q] = (act[q] - m->DisGradAvg_t[q]) / d.dt;
-        }
-        for (int q = 0; q < 9; ++q) {
-            m->VelGradAvg[q] = vga[q];
-            m->DisGradAvg_t[q] = act[q];
-            m->DisGradAvg[q] = act[q] + d.Udot[q] * d.dt;
-        }
+    if (lane == 0) {
+        m->iter = it + 1;
+        m->iter_total += 1;
+        m->nr_total += tot[14];
+        m->nr_max = max(m->nr_max, (int)tot[15]);
+        const double *dg = s_dg;
+        double t6[6] = {dg[0], dg[4], dg[8], 0.5 * (dg[5] + dg[7]), 0.5 * (dg[2] + dg[6]), 0.5 * (dg[1] + dg[3])};
+        t6_to_b<double>(t6, m->ddg6);
+        m->first_iter = 0;
+        m->pending_prelude = 0;
+        m->converged = more ? 0 : 1;
+    }
+    if (more) return;
+    // epilogue macro bookkeeping (evolution.c:438-461); lane q < 9 entry q
+    if (lane < 9) {
+        const int q = lane;
+        const double act = m->DisGradAvg[q] + m->dDisGradAvg_acum[q];
+        const double vga = (act - m->DisGradAvg_t[q]) / d.dt;
+        s_act[0][q] = act;
+        s_act[1][q] = vga;
+        m->VelGradAvg[q] = vga;
+        m->DisGradAvg_t[q] = act;
+        m->DisGradAvg[q] = act + d.Udot[q] * d.dt;
         // the prelude of this increment used the previous DisGradAvg_actual
-        for (int q = 0; q < 9; ++q) {
-            m->DGA_prev[q] = m->DisGradAvg_actual[q];
-            m->DisGradAvg_actual[q] = act[q];
-        }
-        m->e_vm = vm_strain(act);
-        m->d_vm = vm_strain(vga);
+        m->DGA_prev[q] = m->DisGradAvg_actual[q];
+        m->DisGradAvg_actual[q] = act;
+    }
+    __syncwarp();
+    // lane 0: e_vm of DisGradAvg_actual, lane 1: d_vm of VelGradAvg
+    if (lane < 2) {
+        const double v = vm_strain(s_act[lane]);
+        if (lane == 0) m->e_vm = v;
+        else m->d_vm = v;
+    }
+    if (lane == 0) {
         // the displacement gradient received every dDisGradAvg of this
         // increment except the last one, which get_smacro computes after the
         // final update (evolution.c:391 vs :418): only those enter VelGrad
         double a[9];
-        for (int q = 0; q < 9; ++q) a[q] = acum[q] - dg[q];
+        for (int q = 0; q < 9; ++q) a[q] = m->dDisGradAvg_acum[q] - s_dg[q];
         m->acum_a[0] = 0.5 * (a[5] - a[7]);
         m->acum_a[1] = 0.5 * (a[2] - a[6]);
         m->acum_a[2] = 0.5 * (a[1] - a[3]);
     }
+    __syncwarp();
 }
 
 
@@ -1824,7 +2001,10 @@ int nr_resident_blocks(int kind)
             cudaFuncSetAttribute(kb_nr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNrStageBytes);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<true>, VOCE_NR_THREADS, kNrStageBytes);
         } else if (kind == 2) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false, false, true>, VOCE_NR_THREADS, 0);
+            cudaFuncSetAttribute(kb_nr<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kNrStageBytes);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false, false, true>, VOCE_NR_THREADS,
+                                                          kNrStageBytes);
         } else {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, VOCE_NR_THREADS, 0);
         }
@@ -1873,8 +2053,8 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
         kb_nr<true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(1)), VOCE_NR_THREADS, kNrStageBytes, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);
     else if (bp.ir)
-        kb_nr<false, false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(2)), VOCE_NR_THREADS, 0, s>>>(
-            D, bp.map[BP_NP], bp.total[BP_NP]);
+        kb_nr<false, false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(2)), VOCE_NR_THREADS,
+                                    kNrStageBytes, s>>>(D, bp.map[BP_NP], bp.total[BP_NP]);
     else if (bp.mixed)
         kb_nr<false, true><<<grid_for(bp.total[BP_NP], nr_resident_blocks(0)), VOCE_NR_THREADS, 0, s>>>(
             D, bp.map[BP_NP], bp.total[BP_NP]);

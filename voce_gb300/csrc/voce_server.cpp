@@ -82,6 +82,9 @@ int suspend(voce_server *s, Request &q)
     return VOCE_OK;
 }
 
+// End a request: done (error 0), failed (a VOCE_ERR_* code) or cancelled
+// (VOCE_ERR_CANCELLED).  Its RVE leaves the batch and its device memory is
+// freed; a finished request's record and (with keep_fields) fields are kept.
 void retire(voce_server *s, Request &q, int error)
 {
     if (q.rve) {
@@ -105,19 +108,46 @@ void retire(voce_server *s, Request &q, int error)
                 voce_rve_get_field(q.rve, VOCE_FIELD_EDOT_VOIGT, q.edot.data());
             }
         }
-        voce_batch_remove(s->batch, q.rve);
+        if (s->batch) voce_batch_remove(s->batch, q.rve);
         voce_rve_destroy(q.rve);
         q.rve = nullptr;
         s->in_use -= q.footprint;
         s->active -= voxels(q);
     }
-    q.info.status = error ? VOCE_REQ_FAILED : VOCE_REQ_DONE;
+    q.info.status = error == VOCE_ERR_CANCELLED ? VOCE_REQ_CANCELLED : error ? VOCE_REQ_FAILED : VOCE_REQ_DONE;
     q.info.error = error;
     q.info.t_done = s->now();
     // inputs are no longer needed
     std::vector<double>().swap(q.euler);
     std::vector<int>().swap(q.grain);
     std::vector<int>().swap(q.phase);
+    std::vector<char>().swap(q.snap);
+}
+
+bool ended(const Request &q)
+{
+    return q.info.status == VOCE_REQ_DONE || q.info.status == VOCE_REQ_FAILED ||
+           q.info.status == VOCE_REQ_CANCELLED;
+}
+
+// End request q with `error`, wherever it is (queue or batch).
+void end_request(voce_server *s, Request &q, int error)
+{
+    if (q.info.status == VOCE_REQ_QUEUED) {
+        auto it = std::find(s->queue.begin(), s->queue.end(), q.info.id);
+        if (it != s->queue.end()) s->queue.erase(it);
+    } else if (q.info.status == VOCE_REQ_RUNNING) {
+        auto it = std::find(s->running.begin(), s->running.end(), q.info.id);
+        if (it != s->running.end()) s->running.erase(it);
+    }
+    retire(s, q, error);
+}
+
+// The device batch, made at the first admission (a server that has admitted
+// nothing needs no GPU).
+int ensure_batch(voce_server *s)
+{
+    return s->batch ? VOCE_OK : voce_batch_create(s->precision, &s->batch);
 }
 
 }  // namespace
@@ -135,11 +165,6 @@ int voce_server_create(int precision, long long budget, int ticks_per_round, int
     s->budget = budget;
     s->ticks_per_round = ticks_per_round;
     s->keep_fields = keep_fields != 0;
-    int rc = voce_batch_create(s->precision, &s->batch);
-    if (rc) {
-        delete s;
-        return rc;
-    }
     *out = s;
     return VOCE_OK;
 }
@@ -170,9 +195,41 @@ int voce_server_submit(voce_server *s, const voce_namelist *nl, const voce_slip 
     return VOCE_OK;
 }
 
+int voce_server_cancel(voce_server *s, long long id)
+{
+    if (!s) return VOCE_ERR_ARG;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return VOCE_ERR_ARG;
+    Request &q = *it->second;
+    if (ended(q)) return VOCE_ERR_STATE;
+    end_request(s, q, VOCE_ERR_CANCELLED);
+    return VOCE_OK;
+}
+
+int voce_server_set_deadline(voce_server *s, long long id, double t)
+{
+    if (!s || !(t >= 0.0)) return VOCE_ERR_ARG;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return VOCE_ERR_ARG;
+    if (ended(*it->second)) return VOCE_ERR_STATE;
+    it->second->info.t_deadline = t;
+    return VOCE_OK;
+}
+
 int voce_server_poll(voce_server *s, int *running, int *queued)
 {
     if (!s) return VOCE_ERR_ARG;
+    // requests past their deadline end first (queued or running; between
+    // ticks, so none of their kernels is in flight)
+    {
+        const double now = s->now();
+        std::vector<long long> late;
+        for (long long id : s->queue)
+            if (s->reqs[id]->info.t_deadline > 0.0 && now >= s->reqs[id]->info.t_deadline) late.push_back(id);
+        for (long long id : s->running)
+            if (s->reqs[id]->info.t_deadline > 0.0 && now >= s->reqs[id]->info.t_deadline) late.push_back(id);
+        for (long long id : late) end_request(s, *s->reqs[id], VOCE_ERR_DEADLINE);
+    }
     // admission: first in, first out, while the footprint fits (and the
     // voxels in flight stay under the active limit, when one is set: a lone
     // request is always admitted); with a quantum, requests that have run
@@ -198,7 +255,11 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
             continue;
         }
         s->queue.pop_front();
-        int rc = VOCE_OK;
+        int rc = ensure_batch(s);
+        if (rc != VOCE_OK) {
+            retire(s, q, rc);
+            continue;
+        }
         if (!q.snap.empty()) {
             // a suspended request: its state comes back from the snapshot
             rc = voce_rve_restore(q.snap.data(), (long long)q.snap.size(), &q.rve);
@@ -294,10 +355,10 @@ int voce_server_destroy(voce_server *s)
     if (!s) return VOCE_OK;
     for (auto &kv : s->reqs)
         if (kv.second->rve) {
-            voce_batch_remove(s->batch, kv.second->rve);
+            if (s->batch) voce_batch_remove(s->batch, kv.second->rve);
             voce_rve_destroy(kv.second->rve);
         }
-    voce_batch_destroy(s->batch);
+    if (s->batch) voce_batch_destroy(s->batch);
     delete s;
     return VOCE_OK;
 }
