@@ -91,6 +91,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="cfg2: the FP64 line only (no forms / batched / served keys)")
+    p.add_argument("--no-cpu", action="store_true", help="cfg2: no CPU baseline sample")
+    p.add_argument("--forms", default="",
+                   help="cfg3: comma-separated forms to run (default: all)")
     p.add_argument("--extra-rves", type=int, default=512, help="cfg2 line: RVEs of the batched key")
     p.add_argument("--extra-requests", type=int, default=200,
                    help="cfg2 line: requests of the served key")
@@ -458,11 +461,11 @@ def run_voce(args, rank, world, grp):
 
     # ---- CPU baseline (rank 0, N=1 only) ---------------------------------
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, n_it = cpu_sample(threads, 2)
+        v, dt, n_it = cpu_sample(threads, 1)
         cpu = {"value": v, "unit": "voxel-iter/s", "cores": threads, "kind": "port",
-               "sample": "the first 2 whole increments of the same 64^3 case (%d Green iterations, "
+               "sample": "the first whole increment of the same 64^3 case (%d Green iterations, "
                          "%.1f s on %d threads); --impl reference times the increments this line "
                          "times" % (n_it, dt, threads)}
 
@@ -577,7 +580,10 @@ def run_cfg3(args):
     nv = case.mesh.nvox
     out = {}
     lib = capi.load()
-    for name in ("fp64", "mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32"):
+    names = [f for f in args.forms.split(",") if f] if args.forms else list(FORMS)
+    if chosen not in names:
+        names.append(chosen)
+    for name in names:
         lib.voce_set_ir_predictor(0 if name == "mixed_ir_strict" else 1)
         try:
             r = capi.Rve.create(nl, slip, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase,
@@ -608,11 +614,13 @@ def run_cfg3(args):
         y = np.asarray(y, float)
         return float(np.abs(x - y).max() / np.abs(y).max())
 
-    b = out["fp64"]
-    forms = {"fp64": {"value": b["value"], "ms_per_step": b["ms"] / args.steps, "iters": b["iters"],
-                      "kernel_us_per_iteration": b["kernel_us_per_iteration"]}}
-    for name in ("mixed", "mixed_ir", "mixed_ir_strict", "mixed_nr32"):
-        a = out[name]
+    b = out.get("fp64")
+    forms = {}
+    for name, a in out.items():
+        if name == "fp64" or b is None:
+            forms[name] = {"value": a["value"], "ms_per_step": a["ms"] / args.steps, "iters": a["iters"],
+                           "kernel_us_per_iteration": a["kernel_us_per_iteration"]}
+            continue
         forms[name] = {
             "value": a["value"], "ms_per_step": a["ms"] / args.steps, "iters": a["iters"],
             "kernel_us_per_iteration": a["kernel_us_per_iteration"],

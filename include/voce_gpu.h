@@ -219,7 +219,9 @@ int voce_rve_get_field(voce_rve *r, int field, double *host_out);
  *     VOCE_ERR_UNSUPPORTED; voce_rve_get_field has no such limit.  Every field
  *     of an RVE up to 64^3 fits, and 1-wide fields up to 4 Mi voxels.
  *   - The first call on a device does its set-up (looks up the array's device
- *     address); make that first call before any stream capture.
+ *     address); make that first call before any stream capture.  The address
+ *     is kept for the life of the process: a device reset (cudaDeviceReset)
+ *     after that first call is not supported.
  *   - All calls on a device share the array, which keeps the last call's
  *     contents.  Each call writes every value it reads back, so nothing needs
  *     clearing, but calls whose work overlaps on the GPU (threads downloading

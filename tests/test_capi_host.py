@@ -91,7 +91,7 @@ def test_footprint_scales_with_grid(voce_lib):
     # (the FP64 form also stores n and omega of every frequency: 9 doubles)
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED) == a - 9 * 8 * nspec - 9 * 8 * nspec
     assert capi.footprint((64, 64, 64), capi.PREC_MIXED_NR32) == a + 840 * nv - 2 * 9 * 8 * nspec
-    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_IR) == a + 840 * nv - 2 * 9 * 8 * nspec
+    assert capi.footprint((64, 64, 64), capi.PREC_MIXED_IR) == a + (840 + 168) * nv - 2 * 9 * 8 * nspec
     assert capi.footprint((256, 256, 256)) < 40e9
 
 

@@ -437,6 +437,8 @@ int alloc_device(voce_rve *r)
     d.itau32 = nullptr;
     d.sgp32 = nullptr;
     d.sch_lo = d.itau_lo = d.sgp_lo = nullptr;
+    d.sgp = nullptr;
+    if (d.ir) AL(d.sgp, 21 * nv);
     if (d.nr32 || d.ir) {
         AL(d.sch32, 60 * nv); AL(d.itau32, 24 * nv); AL(d.sgp32, 21 * nv);
         AL(d.sch_lo, 60 * nv); AL(d.itau_lo, 24 * nv); AL(d.sgp_lo, 21 * nv);
@@ -486,6 +488,7 @@ void for_state(RveDesc &d, F &&f)
     f((void **)&d.taux, 12 * nv * D);    f((void **)&d.svm, nv * D);
     f((void **)&d.evm, nv * D);          f((void **)&d.rotl, 3 * nv * D);
     f((void **)&d.diag, 3 * nv * D);     f((void **)&d.phase, nv * sizeof(int));
+    if (d.ir) f((void **)&d.sgp, 21 * nv * D);
     if (d.nr32 || d.ir) {
         f((void **)&d.sch32, 60 * nv * S);
         f((void **)&d.itau32, 24 * nv * S);
@@ -514,8 +517,9 @@ long long voce_rve_footprint(const int dims[3], int precision)
     // svm 1, evm 1, rotl 3, diag 3  (= 214) + phase (4 bytes)
     // + the FP64 form's stored Green-operator frequencies, 9 doubles each
     // + the mixed_nr32 and mixed_ir forms' float pairs of sch, itau and
-    // S_g + S0 (2 x 105 floats)
-    const long long f32 = (precision == VOCE_PREC_MIXED_NR32 || precision == VOCE_PREC_MIXED_IR) ? 840 : 0;
+    // S_g + S0 (2 x 105 floats), and the mixed_ir form's S_g + S0 in FP64 (21
+    // doubles)
+    const long long f32 = precision == VOCE_PREC_MIXED_NR32 ? 840 : precision == VOCE_PREC_MIXED_IR ? 840 + 168 : 0;
     return nv * (214 * 8 + 4 + f32) + nspec * 9 * cplx +
            (precision == VOCE_PREC_FP64 ? nspec * 9 * 8 : 0);
 }

@@ -11,6 +11,7 @@
 //   tm[9][nv]     crystal->sample rotation TranMat_xt2sa (evp.h:240)
 //   sch[60][nv]   Schmid 5-vectors of the 12 systems in sample axes
 //   sg[21][nv]    grain compliance S_g = C_gr^-1, packed upper triangle
+//   sgp[21][nv]   S_g + S0, packed (mixed_ir form only)
 //   crss[24][nv]  critical resolved shear stress (system, +/- direction)
 //   itau[24][nv]  1/crss
 //   gamacum[nv], gtot[12][nv], edot[5][nv], gamdot[12][nv], taux[12][nv],
@@ -122,6 +123,7 @@ struct RveDesc {
     float *itau32;       // float copy of itau (float-Jacobian Newton forms only)
     float *sgp32;        // float (S_g + S0), packed upper triangle (float-Jacobian Newton forms only)
     float *sch_lo, *itau_lo, *sgp_lo;   // x - (double)x32 rounded to float, for the same three
+    double *sgp;         // S_g + S0 in FP64, packed upper triangle (the mixed_ir Newton's residual)
     double *gamacum, *gtot, *edot, *gamdot, *taux, *svm, *evm, *rotl, *diag;
     int *phase;
     void *spec, *aacc;

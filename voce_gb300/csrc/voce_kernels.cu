@@ -921,16 +921,23 @@ __device__ __forceinline__ bool ir_start(const RveDesc &d, long long v, const fl
     ++it;
 #pragma unroll
     for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c] - (double)x[c];
+    // the staged column is read no more: it keeps the last matrix for the
+    // FP64 steps (st is this thread's own column)
+    float *mst = const_cast<float *>(st);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) mst[sym6(i, j) * VOCE_NR_THREADS] = Mf[i][j];
     return true;
 }
 
 // One FP64-Jacobian step of newton_ir, for the rare iteration whose
 // resolved-shear ratio leaves the float range; kept out of line so that its
 // registers do not weigh on the common path.
-__device__ __noinline__ void ir_fp64_step(const RveDesc &d, long long v, const double *P, const double *sig,
-                                          double *R)
+__device__ __noinline__ void ir_fp64_step(const RveDesc &d, long long v, const double *sig, double *R)
 {
-    double Dd[15], edd[5];
+    double P[21], Dd[15], edd[5];
+    for (int q = 0; q < 21; ++q) P[q] = d.sgp[(long long)q * d.nv + v];
     flow_rule<true, false, double>(d, v, sig, edd, Dd, nullptr, nullptr);
     double M[6][6], b[6];
 #pragma unroll
@@ -948,9 +955,17 @@ __device__ __noinline__ void ir_fp64_step(const RveDesc &d, long long v, const d
     for (int i = 0; i < 6; ++i) R[i] = b[i];
 }
 
-__device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const double (&P)[21],
-                                          const double (&cc)[6], double thr, double (&sig)[6],
-                                          double (&sp)[6], double (&Rl)[6], int &it)
+// mst (with START): the single-precision matrix of the start's last step,
+// lower triangle packed, in the voxel's staged column; the FP64 steps solve
+// with it instead of assembling the Jacobian again (near the root it is the
+// Jacobian to about n x 1e-4 relative, so each step still divides the error
+// by ~500 -- and from the start one step is usually the last).  S_g + S0 is
+// read from d.sgp (FP64, stored at setup) where the residual needs it, rather
+// than kept in registers across the iterations.
+template <bool START>
+__device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const double (&cc)[6],
+                                          double thr, double (&sig)[6], double (&sp)[6],
+                                          double (&Rl)[6], int &it, const float *mst)
 {
     const long long nv = d.nv;
     const double dtg = d.dt * d.gam0[0];
@@ -967,6 +982,7 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
 #pragma unroll
         for (int q = 0; q < 15; ++q) D[q] = 0.0f;
         bool big = false;
+#pragma unroll 2
         for (int k = 0; k < d.nsys; ++k) {
             double sc[5];
 #pragma unroll
@@ -974,13 +990,16 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
             const double rss = sc[0] * sig[0] + sc[1] * sig[1] + sc[2] * sig[2] + sc[3] * sig[3] + sc[4] * sig[4];
             const int neg = __double2hiint(rss) < 0;
             const long long ti = (long long)(2 * k + neg) * nv + v;
-            const double r = rss * __ldg(d.itau + ti);
+            const double it0 = __ldg(d.itau + (long long)(2 * k) * nv + v);
+            const double it1 = __ldg(d.itau + (long long)(2 * k + 1) * nv + v);
+            const double r = rss * (neg ? it1 : it0);
             const double a = fabs(r);
             const double ae = pow_abs_e(a, e);        // |r|^(n-1)
             const double g2 = ae * r;                 // |r|^n sign(r) / gam0
 #pragma unroll
             for (int i = 0; i < 5; ++i) ed[i] = fma(sc[i], g2, ed[i]);
             big = big || !(a < 60.0);
+            if (START) continue;
             // Jacobian term gam0 n |r|^(n-1) / tau m m^T, in single precision
             const float g1 = g1c * (float)ae * __ldg(d.itau32 + ti);
             float sf[5], t[5];
@@ -1000,7 +1019,7 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
         for (int i = 0; i < 6; ++i) {
             double s = (i < 5) ? fma(dtg, ed[i], cc[i]) : cc[i];
 #pragma unroll
-            for (int j = 0; j < 6; ++j) s = fma(P[sym6(i, j)], sig[j], s);
+            for (int j = 0; j < 6; ++j) s = fma(__ldg(d.sgp + (long long)sym6(i, j) * nv + v), sig[j], s);
             R[i] = s;
             Rl[i] = s;
         }
@@ -1011,8 +1030,13 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
                 x[i] = (float)R[i];
 #pragma unroll
                 for (int j = 0; j <= i; ++j) {
-                    float m = __ldg(d.sgp32 + (long long)sym6(i, j) * nv + v);
-                    if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    float m;
+                    if (START) {
+                        m = mst[sym6(i, j) * VOCE_NR_THREADS];
+                    } else {
+                        m = __ldg(d.sgp32 + (long long)sym6(i, j) * nv + v);
+                        if (i < 5 && j < 5) m = fmaf(dtf, D[j * 5 - (j * (j - 1)) / 2 + (i - j)], m);
+                    }
                     M[i][j] = m;
                 }
             }
@@ -1020,7 +1044,7 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
 #pragma unroll
             for (int i = 0; i < 6; ++i) R[i] = (double)x[i];
         } else {
-            ir_fp64_step(d, v, P, sig, R);
+            ir_fp64_step(d, v, sig, R);
         }
         double cnr = 0.0;
 #pragma unroll
@@ -1105,23 +1129,26 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
         if (NR32) {
             mixed_newton(d, v, st, lam, cc, sn2, polish, sig, sp, Rl, it);
             cp_async_wait_all();   // (already done unless the float phase was skipped)
+        } else if (IR && d.ipow_n >= 1) {
+            // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
+            bool started = false;
+            if (d.ir_pred) {
+                int it0 = it;
+                started = ir_start(d, v, st, lam, cc, sn2, sig, it);
+                if (!started) {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) sig[c] = lam[c];
+                    it = it0;
+                }
+            }
+            if (started) newton_ir<true>(d, v, cc, 1e-14 * sn2, sig, sp, Rl, it, st);
+            else newton_ir<false>(d, v, cc, 1e-14 * sn2, sig, sp, Rl, it, nullptr);
+            cp_async_wait_all();
         } else {
             double P[21];
             load_P(d, v, P);
             // sqrt(cnr)/signorm > 1e-7 (evolution.c:112) tested as cnr > 1e-14 signorm^2
-            if (IR && d.ipow_n >= 1) {
-                if (d.ir_pred) {
-                    int it0 = it;
-                    if (!ir_start(d, v, st, lam, cc, sn2, sig, it)) {
-#pragma unroll
-                        for (int c = 0; c < 6; ++c) sig[c] = lam[c];
-                        it = it0;
-                    }
-                }
-                newton_ir(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
-            } else {
-                newton_fp64<IR, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
-            }
+            newton_fp64<IR, CHORD>(d, v, P, cc, 1e-14 * sn2, sig, sp, Rl, it);
             if (IR) cp_async_wait_all();
         }
         double ncs, nce;   // |sig - lam| and the strain-compatibility norm (evolution.c:118-123)
@@ -1813,8 +1840,11 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
 // CHORD: the FP64 Newton may take chord steps (VOCE_PREC_MIXED plans; each
 // RVE's d.chord decides); the FP64 form's instance is the exact-Jacobian one
 // IR: the VOCE_PREC_MIXED_IR form (FP64 residual, float Jacobian)
+#ifndef VOCE_NR_IR_BLOCKS
+#define VOCE_NR_IR_BLOCKS 3
+#endif
 template <bool NR32, bool CHORD = false, bool IR = false>
-__global__ void __launch_bounds__(128, NR32 ? VOCE_NR_MIXED_BLOCKS : 1)
+__global__ void __launch_bounds__(128, NR32 ? VOCE_NR_MIXED_BLOCKS : IR ? VOCE_NR_IR_BLOCKS : 1)
 kb_nr(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
@@ -2269,6 +2299,8 @@ __global__ void k_fill_p32(RveDesc d)
         load_P(d, v, P);
         const bool solid = d.solid[d.phase[v]] != 0;
         for (int q = 0; q < 21; ++q) put_pair(d.sgp32, d.sgp_lo, (long long)q * d.nv + v, solid ? P[q] : 0.0);
+        if (d.sgp)
+            for (int q = 0; q < 21; ++q) d.sgp[(long long)q * d.nv + v] = solid ? P[q] : 0.0;
     }
 }
 
