@@ -40,8 +40,8 @@
  * EpsAvg, EdotAvg, DisGradAvg.
  *
  * One grid runs on one GPU: under mpirun only rank 0 does the work and the
- * other ranks return at once.  VOCE_PRECISION=mixed in the environment
- * selects the mixed-precision form.  A failure prints "voce: <message>" on
+ * other ranks return at once.  VOCE_PRECISION=mixed, mixed_ir or mixed_nr32
+ * in the environment selects that precision form (FP64 otherwise).  A failure prints "voce: <message>" on
  * stderr and exits, with status 35 for a singular matrix (the reference's
  * exit(35), kinematics.c:306-309) and 1 otherwise.
  */

@@ -164,7 +164,10 @@ void voce_legacy_setup(void)
     mesh.grain = grain_f;
     mesh.phase = phase_f;
     const char *pe = std::getenv("VOCE_PRECISION");
-    const int prec = (pe && std::strcmp(pe, "mixed") == 0) ? VOCE_PREC_MIXED : VOCE_PREC_FP64;
+    int prec = VOCE_PREC_FP64;
+    if (pe && std::strcmp(pe, "mixed") == 0) prec = VOCE_PREC_MIXED;
+    else if (pe && std::strcmp(pe, "mixed_ir") == 0) prec = VOCE_PREC_MIXED_IR;
+    else if (pe && std::strcmp(pe, "mixed_nr32") == 0) prec = VOCE_PREC_MIXED_NR32;
     check(voce_rve_create(&nl, sp, &mesh, prec, &g_rve));
 
     // one rank holds the whole grid (init.c:647 with one process)
