@@ -255,28 +255,61 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
 // ---------------------------------------------------------------------------
 // FFT passes
 // ---------------------------------------------------------------------------
-// Tile copy of n elements by the block: each thread first loads U elements
-// (i, i + nthr, ...) into registers, then stores them, so that U global loads
-// per thread are in flight at once instead of one load-store pair at a time.
-// ld(i) returns element i, st(i, value) places it.
+// Position (a0, a1, a2) of a flat tile index i = a0 + n0 (a1 + n1 a2),
+// carried from one element of a thread to its next (i += step) by additions
+// and compares: a tile loop pays the integer divisions by the run-time tile
+// extents once per thread instead of once per element (those divisions were
+// most of the instructions of the FFT passes' load and store loops).
+struct Idx3 {
+    int a0, a1, a2, d0, d1, d2, n0, n1;
+    __device__ __forceinline__ Idx3(int i, int step, int n0_, int n1_) : n0(n0_), n1(n1_)
+    {
+        int t = i / n0;
+        a0 = i - t * n0;
+        a1 = t % n1;
+        a2 = t / n1;
+        t = step / n0;
+        d0 = step - t * n0;
+        d1 = t % n1;
+        d2 = t / n1;
+    }
+    __device__ __forceinline__ void next()
+    {
+        a0 += d0;
+        int c = a0 >= n0;
+        if (c) a0 -= n0;
+        a1 += d1 + c;
+        c = a1 >= n1;
+        if (c) a1 -= n1;
+        a2 += d2 + c;
+    }
+};
+constexpr int kIdxUnbounded = 1 << 30;   // n1 of a two-level index (a2 stays 0)
+
+// Tile copy of n elements by the block over a carried index: each thread
+// first loads U elements (its i, i + nthr, ...) into registers, then stores
+// them, so that U global loads per thread are in flight at once.
+// ld(a0, a1, a2) returns an element, st(a0, a1, a2, value) places it.
 template <int U, typename T, class LD, class ST>
-__device__ __forceinline__ void staged_copy(int n, LD ld, ST st)
+__device__ __forceinline__ void staged_copy3(int n, int n0, int n1, LD ld, ST st)
 {
     const int nt = blockDim.x;
+    Idx3 il(threadIdx.x, nt, n0, n1), is = il;
     for (int b = threadIdx.x; b < n; b += U * nt) {
         T v[U];
 #pragma unroll
         for (int j = 0; j < U; ++j) {
-            const int i = b + j * nt;
-            if (i < n) v[j] = ld(i);
+            if (b + j * nt < n) v[j] = ld(il.a0, il.a1, il.a2);
+            il.next();
         }
 #pragma unroll
         for (int j = 0; j < U; ++j) {
-            const int i = b + j * nt;
-            if (i < n) st(i, v[j]);
+            if (b + j * nt < n) st(is.a0, is.a1, is.a2, v[j]);
+            is.next();
         }
     }
 }
+
 // loads in flight per thread: the single-precision passes wait on memory, the
 // double-precision ones on the FP64 pipe (there one at a time, as before,
 // keeps their registers and occupancy)
@@ -300,12 +333,11 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
     const int ytiles = ny / rows;
     const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const long long vb = ((long long)x * ny + y0) * nz;
-    // element idx = (c * rows + r) * nz + z is sig[c][vb + r * nz + z]
-    staged_copy<kZCopyDepth, double>(
-        6 * rows * nz,
-        [&](int idx) { return __ldg(d.sig + (idx / (rows * nz)) * nv + vb + idx % (rows * nz)); },
-        [&](int idx, double v) {
-            const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+    // element (z, r, c) is sig[c][vb + r * nz + z]
+    staged_copy3<kZCopyDepth, double>(
+        6 * rows * nz, nz, rows,
+        [&](int z, int r, int c) { return __ldg(d.sig + c * nv + vb + (long long)r * nz + z); },
+        [&](int z, int r, int c, double v) {
             C *e = &bufA[z * ldl + (c >> 1) * rows + r];
             if (c & 1) e->y = (R)v; else e->x = (R)v;
         });
@@ -313,8 +345,9 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, -1);
     C *spec = (C *)d.spec;
     const long long plane = (long long)nx * ny;
-    for (int idx = threadIdx.x; idx < 3 * rows * nzh; idx += blockDim.x) {
-        const int r = idx % rows, t = idx / rows, k = t % nzh, p = t / nzh;
+    Idx3 ix(threadIdx.x, blockDim.x, rows, nzh);
+    for (int idx = threadIdx.x; idx < 3 * rows * nzh; idx += blockDim.x, ix.next()) {
+        const int r = ix.a0, k = ix.a1, p = ix.a2;
         const int l = p * rows + r;
         const C zk = res[k * ldl + l], zm = res[((nz - k) % nz) * ldl + l];
         C A, B;
@@ -346,8 +379,9 @@ __device__ void fft_z_fwd_src(const RveDesc &d, const double *src, void *dstp, i
     const int ytiles = ny / rows;
     const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const long long vb = ((long long)x * ny + y0) * nz;
-    for (int idx = threadIdx.x; idx < 2 * np * rows * nz; idx += blockDim.x) {
-        const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+    Idx3 iz(threadIdx.x, blockDim.x, nz, rows);
+    for (int idx = threadIdx.x; idx < 2 * np * rows * nz; idx += blockDim.x, iz.next()) {
+        const int z = iz.a0, r = iz.a1, c = iz.a2;
         const R val = (ncomp % 2 == 0 || c < ncomp) ? (R)__ldg(src + c * nv + vb + (long long)r * nz + z) : R(0);
         C *e = &bufA[z * ldl + (c >> 1) * rows + r];
         if (c & 1) e->y = val; else e->x = val;
@@ -356,8 +390,9 @@ __device__ void fft_z_fwd_src(const RveDesc &d, const double *src, void *dstp, i
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, -1);
     C *spec = (C *)dstp;
     const long long plane = (long long)nx * ny;
-    for (int idx = threadIdx.x; idx < np * rows * nzh; idx += blockDim.x) {
-        const int r = idx % rows, t = idx / rows, k = t % nzh, p = t / nzh;
+    Idx3 ix(threadIdx.x, blockDim.x, rows, nzh);
+    for (int idx = threadIdx.x; idx < np * rows * nzh; idx += blockDim.x, ix.next()) {
+        const int r = ix.a0, k = ix.a1, p = ix.a2;
         const int l = p * rows + r;
         const C zk = res[k * ldl + l], zm = res[((nz - k) % nz) * ldl + l];
         C A, B;
@@ -387,15 +422,15 @@ __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int 
     const int x0 = (unit % xtiles) * xt;
     C *spec = (C *)specp;
     const long long base = ((long long)line * nx + x0) * ny;
-    staged_copy<CopyDepth<R>::v, C>(
-        xt * ny, [&](int idx) { return spec[base + idx]; },
-        [&](int idx, C v) { bufA[(idx % ny) * ldl + idx / ny] = v; });
+    // element (y, xl) is spec[base + xl * ny + y]
+    staged_copy3<CopyDepth<R>::v, C>(
+        xt * ny, ny, kIdxUnbounded, [&](int y, int xl, int) { return spec[base + xl * ny + y]; },
+        [&](int y, int xl, int, C v) { bufA[y * ldl + xl] = v; });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.ply, (const C *)d.twy, sign);
-    for (int idx = threadIdx.x; idx < xt * ny; idx += blockDim.x) {
-        const int xl = idx / ny, y = idx % ny;
-        spec[base + idx] = res[y * ldl + xl];
-    }
+    Idx3 ix(threadIdx.x, blockDim.x, ny, kIdxUnbounded);
+    for (int idx = threadIdx.x; idx < xt * ny; idx += blockDim.x, ix.next())
+        spec[base + idx] = res[ix.a0 * ldl + ix.a1];
 }
 
 
@@ -414,22 +449,18 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     C *aacc = (C *)d.aacc;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
-    staged_copy<CopyDepth<R>::v, C>(
-        6 * nx * kc,
-        [&](int idx) {
-            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-            return spec[c * cstride + kb + (long long)x * ny + yl];
-        },
-        [&](int idx, C v) {
-            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-            bufA[x * ldl + c * kc + yl] = v;
-        });
+    // element (yl, x, c) is spec[c][kz][x][y0 + yl]
+    staged_copy3<CopyDepth<R>::v, C>(
+        6 * nx * kc, kc, nx,
+        [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
+        [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, -1);
     C *oth = (res == bufA) ? bufB : bufA;
     const int first = d.macro->first_iter;
-    for (int idx = threadIdx.x; idx < nx * kc; idx += blockDim.x) {
-        const int yl = idx % kc, x = idx / kc;
+    Idx3 ig(threadIdx.x, blockDim.x, kc, kIdxUnbounded);
+    for (int idx = threadIdx.x; idx < nx * kc; idx += blockDim.x, ig.next()) {
+        const int yl = ig.a0, x = ig.a1;
         R br[6], bi[6], ar[3], ai[3];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
@@ -460,8 +491,9 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     }
     __syncthreads();
     C *res2 = fft_lines<R>(res, oth, NL, ldl, d.plx, (const C *)d.twx, +1);
-    for (int idx = threadIdx.x; idx < 6 * nx * kc; idx += blockDim.x) {
-        const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+    Idx3 is(threadIdx.x, blockDim.x, kc, nx);
+    for (int idx = threadIdx.x; idx < 6 * nx * kc; idx += blockDim.x, is.next()) {
+        const int yl = is.a0, x = is.a1, c = is.a2;
         spec[c * cstride + kb + (long long)x * ny + yl] = res2[x * ldl + c * kc + yl];
     }
 }
@@ -481,20 +513,15 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
     C *spec = (C *)specp;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
-    staged_copy<CopyDepth<R>::v, C>(
-        ncomp * nx * kc,
-        [&](int idx) {
-            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-            return spec[c * cstride + kb + (long long)x * ny + yl];
-        },
-        [&](int idx, C v) {
-            const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
-            bufA[x * ldl + c * kc + yl] = v;
-        });
+    staged_copy3<CopyDepth<R>::v, C>(
+        ncomp * nx * kc, kc, nx,
+        [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
+        [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, sign);
-    for (int idx = threadIdx.x; idx < ncomp * nx * kc; idx += blockDim.x) {
-        const int yl = idx % kc, t = idx / kc, x = t % nx, c = t / nx;
+    Idx3 is(threadIdx.x, blockDim.x, kc, nx);
+    for (int idx = threadIdx.x; idx < ncomp * nx * kc; idx += blockDim.x, is.next()) {
+        const int yl = is.a0, x = is.a1, c = is.a2;
         spec[c * cstride + kb + (long long)x * ny + yl] = res[x * ldl + c * kc + yl];
     }
 }
@@ -523,10 +550,10 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
     const long long xy = (long long)x * ny + y0;
     const int half = nz / 2;
     struct AB { C a, b; };
-    staged_copy<kZCopyDepth, AB>(
-        np * nz * rows,
-        [&](int idx) {
-            const int r = idx % rows, t = idx / rows, k = t % nz, p = t / nz;
+    // element (r, k, p): line p's coefficient k of row r
+    staged_copy3<kZCopyDepth, AB>(
+        np * nz * rows, rows, nz,
+        [&](int r, int k, int p) {
             const int ca = 2 * p, cb = 2 * p + 1;
             const int ks = k <= half ? k : nz - k;
             const long long o = (long long)ks * plane + xy + r;
@@ -536,8 +563,7 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
             else { v.b.x = R(0); v.b.y = R(0); }
             return v;
         },
-        [&](int idx, AB v) {
-            const int r = idx % rows, t = idx / rows, k = t % nz, p = t / nz;
+        [&](int r, int k, int p, AB v) {
             const bool lo = k <= half;
             C A = v.a, B = v.b;
             if (k == 0 || k == half) { A.y = R(0); B.y = R(0); }
@@ -553,19 +579,19 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
     const double inv = d.inv_nv;
     if (mode == 0) {
         const MacroDev *m = d.macro;
-        // element idx = (c * rows + r) * nz + z is dgs[c][vb + r * nz + z]
-        staged_copy<kZCopyDepth, double>(
-            ncomp * rows * nz,
-            [&](int idx) { return d.dgs[(idx / (rows * nz)) * nv + vb + idx % (rows * nz)]; },
-            [&](int idx, double old) {
-                const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+        // element (z, r, c) is dgs[c][vb + r * nz + z]
+        staged_copy3<kZCopyDepth, double>(
+            ncomp * rows * nz, nz, rows,
+            [&](int z, int r, int c) { return d.dgs[(long long)c * nv + vb + (long long)r * nz + z]; },
+            [&](int z, int r, int c, double old) {
                 const C e = res[z * ldl + (c >> 1) * rows + r];
                 const double val = (double)((c & 1) ? e.y : e.x);
                 d.dgs[(long long)c * nv + vb + (long long)r * nz + z] = old + (m->ddg6[c] + val * inv);
             });
     } else if (mode == 1) {
-        for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x) {
-            const int z = idx % nz, t = idx / nz, r = t % rows, c = t / rows;
+        Idx3 iz(threadIdx.x, blockDim.x, nz, rows);
+        for (int idx = threadIdx.x; idx < ncomp * rows * nz; idx += blockDim.x, iz.next()) {
+            const int z = iz.a0, r = iz.a1, c = iz.a2;
             const C e = res[z * ldl + (c >> 1) * rows + r];
             const double val = (double)((c & 1) ? e.y : e.x);
             d.rotl[(long long)c * nv + vb + (long long)r * nz + z] = val * inv;
