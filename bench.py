@@ -92,6 +92,9 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="cfg2: the FP64 line only (no forms / batched / served keys)")
     p.add_argument("--no-cpu", action="store_true", help="cfg2: no CPU baseline sample")
+    p.add_argument("--no-tune", action="store_true",
+                   help="fixed-budget FFT tiles, no tuning launches (profiler runs: the first "
+                        "kernel launches a profiler sees are then the solve's own)")
     p.add_argument("--forms", default="",
                    help="cfg3: comma-separated forms to run (default: all)")
     p.add_argument("--extra-rves", type=int, default=512, help="cfg2 line: RVEs of the batched key")
@@ -944,6 +947,9 @@ def run_cfg5(args):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.no_tune and args.impl == "voce":
+        from voce_gb300 import capi
+        capi.load().voce_set_autotune(0)
     if args.impl == "voce" and args.config in ("cfg3", "cfg4", "cfg5"):
         {"cfg3": run_cfg3, "cfg4": run_cfg4, "cfg5": run_cfg5}[args.config](args)
         return

@@ -59,6 +59,13 @@ int voce_device_memory(long long *free_bytes, long long *total_bytes);
  * outside 2^-99 <= |x| < 2^99), computed on the current device for n host
  * values: a check of that reciprocal against 1/x. */
 int voce_diag_rcp(const double *x, double *out, int n);
+/* The single-precision line FFT of the spectrum passes on the current
+ * device: nlines lines of length L, in and out [nlines][L] complex values as
+ * interleaved (re, im) doubles (rounded to float on the way in), transformed
+ * by candidate `schedule` of a single-precision axis of length L (see the
+ * schedules below; 0 is the default), sign -1 forward, +1 inverse,
+ * unnormalised.  2 L (nlines | 1) complex floats must fit in 200 KB. */
+int voce_diag_fft(int L, int nlines, int sign, int schedule, const double *in, double *out);
 
 /* FFT tile tuning.  voce_rve_create times the forward-pass FFT phases with
  * a few tile sizes (lines per block) on the new RVE and keeps the fastest,
@@ -76,15 +83,19 @@ int voce_rve_get_tiles(const voce_rve *r, int tiles[6]);
 int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
 
 /* FFT radix schedules (no counterpart in the reference, which leaves its
- * transforms to FFTW).  Each axis of length L = 2^a 3^b runs as Stockham
+ * transforms to FFTW).  Each axis of length L = 2^a 3^b can run as Stockham
  * passes of radix 4, 2 and 3; the candidate schedules are their stage orders
- * 4s-2-3s (the default), 3s-4s-2, 2-4s-3s and 3s-2-4s, duplicates dropped.
+ * 4s-2-3s, 3s-4s-2, 2-4s-3s and 3s-2-4s, duplicates dropped.  In the
+ * single-precision spectrum forms (VOCE_PREC_MIXED, VOCE_PREC_MIXED_NR32,
+ * VOCE_PREC_MIXED_IR) an axis of length 16, 24, 32, 48, 64, 96, 128, 192 or
+ * 256 has one more candidate, placed first: the register FFT, two passes of
+ * small DFTs of lengths N1 x N2 = L held in registers (4x4, 4x6, 4x8, 6x8,
+ * 8x8, 8x12, 8x16, 12x16, 16x16).  Candidate 0 is the default.
  * Unlike the tiles, the schedule changes results in the last bits (a
  * different order of roundings).  So the FP64 form never tunes it: its RVEs
  * run the default schedule of every axis unless the caller sets one, and its
  * results are the same bits in every process.  For the single-precision
- * spectrum forms (VOCE_PREC_MIXED, VOCE_PREC_MIXED_NR32, VOCE_PREC_MIXED_IR),
- * with tuning on,
+ * spectrum forms, with tuning on,
  * voce_rve_create times the candidates of each axis on the forward pass that
  * transforms it (with the tuned tile) and keeps one only when it is more than
  * 3 % faster than the default; the choice is cached with the tiles (and in
@@ -92,12 +103,16 @@ int voce_rve_set_tiles(voce_rve *r, const int tiles[6]);
  * tuning timed differently (within the form's single-precision error), but
  * not within a process: an RVE keeps its schedule for life, alone, in a
  * batch, in the server and through snapshots.
- * voce_fft_schedule_count: candidates for length L (0 if not 2^a 3^b).
- * voce_rve_get_fft_schedule: the radices of axis (0 x, 1 y, 2 z) in stage
- * order; returns the number of stages (at most max written), < 0 on error.
+ * voce_fft_schedule_count: Stockham candidates for length L (the FP64 form's
+ * list; 0 if L is not 2^a 3^b).
+ * voce_rve_fft_schedule_count: the candidates of axis (0 x, 1 y, 2 z) of r.
+ * voce_rve_get_fft_schedule: the radices of axis in stage order (the
+ * register FFT: its two lengths N1, N2); returns the number of stages (at
+ * most max written), < 0 on error.
  * voce_rve_set_fft_schedule: use candidate k of axis; between calls,
  * outside a batch. */
 int voce_fft_schedule_count(int L);
+int voce_rve_fft_schedule_count(const voce_rve *r, int axis);
 /* Chord steps in the FP64 Newton of the VOCE_PREC_MIXED form (no
  * counterpart in the reference, which refreshes the Jacobian every Newton
  * iteration, evolution.c:85-110): once a step has moved the stress by less

@@ -127,6 +127,7 @@ PROTOTYPES = [
     ("voce_measure_fp64_tflops", C.c_double, []),
     ("voce_device_memory", C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     ("voce_diag_rcp", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
+    ("voce_diag_fft", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     # voce_batch.h
     ("voce_batch_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     ("voce_batch_add", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
@@ -161,6 +162,7 @@ PROTOTYPES = [
     ("voce_rve_get_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_rve_set_tiles", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_fft_schedule_count", C.c_int, [C.c_int]),
+    ("voce_rve_fft_schedule_count", C.c_int, [C.c_void_p, C.c_int]),
     ("voce_set_newton_chord", C.c_int, [C.c_int]),
     ("voce_set_ir_predictor", C.c_int, [C.c_int]),
     ("voce_rve_get_fft_schedule", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]),
@@ -264,6 +266,15 @@ def diag_rcp(x: np.ndarray) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.float64)
     out = np.empty_like(x)
     _check(load().voce_diag_rcp(_dptr(x), _dptr(out), x.size))
+    return out
+
+
+def diag_fft(x: np.ndarray, sign: int = -1, schedule: int = 0) -> np.ndarray:
+    """The single-precision line FFT of the spectrum passes (voce_diag_fft)
+    of every row of the complex array x [nlines, L], unnormalised."""
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    out = np.empty_like(x)
+    _check(load().voce_diag_fft(x.shape[1], x.shape[0], sign, schedule, x.ctypes.data, out.ctypes.data))
     return out
 
 
@@ -435,8 +446,16 @@ class Rve:
     def set_tiles(self, tiles) -> None:
         _check(load().voce_rve_set_tiles(self._h, (C.c_int * 6)(*tiles)))
 
+    def fft_schedule_count(self, axis: int) -> int:
+        """Transform candidates of axis (0 x, 1 y, 2 z) of this RVE."""
+        n = load().voce_rve_fft_schedule_count(self._h, axis)
+        if n < 0:
+            _check(-n)
+        return n
+
     def fft_schedule(self, axis: int) -> list:
-        """Radices of axis (0 x, 1 y, 2 z) in stage order."""
+        """Radices of axis (0 x, 1 y, 2 z) in stage order (the register FFT:
+        its two lengths N1, N2)."""
         buf = (C.c_int * 16)()
         n = load().voce_rve_get_fft_schedule(self._h, axis, buf, 16)
         if n < 0:

@@ -185,6 +185,7 @@ bool fft_plan(int L, FftPlan1 &p)
 {
     p.L = L;
     p.nst = 0;
+    p.n1 = 0;
     int m = L;
     while (m % 4 == 0 && p.nst < VOCE_MAXRAD) { p.rad[p.nst++] = 4; m /= 4; }
     while (m % 2 == 0 && p.nst < VOCE_MAXRAD) { p.rad[p.nst++] = 2; m /= 2; }
@@ -211,6 +212,7 @@ int fft_schedules(int L, FftPlan1 *out, int max)
         FftPlan1 p;
         p.L = L;
         p.nst = 0;
+        p.n1 = 0;
         for (int q = 0; q < 3; ++q) {
             const int r = order[o][q], cnt = r == 4 ? n4 : r == 2 ? n2 : n3;
             for (int k = 0; k < cnt; ++k) p.rad[p.nst++] = r;
@@ -221,6 +223,20 @@ int fft_schedules(int L, FftPlan1 *out, int max)
         if (!seen) out[n++] = p;
     }
     return n;
+}
+
+// Transform candidates of an axis of an RVE: for the single-precision
+// spectrum forms, the register FFT first where the length has one
+// (reg_fft_split), then the Stockham schedules; for the FP64 form, the
+// Stockham schedules only.  Candidate 0 is the default.
+int axis_schedules(int L, bool mixed, FftPlan1 *out, int max)
+{
+    int n = 0;
+    if (mixed && max > 0 && reg_fft_split(L) > 0 && fft_plan(L, out[0])) {
+        out[0].n1 = reg_fft_split(L);
+        n = 1;
+    }
+    return n + fft_schedules(L, out + n, max - n);
 }
 
 }  // namespace
@@ -417,6 +433,8 @@ int voce_slip_read(const char *path, voce_slip *out)
 namespace {
 
 int autotune_tiles(voce_rve *r);
+void apply_tiles(voce_rve *r, const Tiles &t);
+Tiles tiles_of(const RveDesc &d);
 extern int g_autotune;
 extern int g_newton_chord;
 extern int g_ir_predictor;
@@ -783,8 +801,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     CUDA_TRY(cudaMemcpyAsync(d.macro, &m, sizeof(m), cudaMemcpyHostToDevice, r->stream));
     if (d.mixed) r->tiles.choose<float>(d);
     else r->tiles.choose<double>(d);
-    d.zrows = r->tiles.zrows; d.yxt = r->tiles.yxt; d.xkc = r->tiles.xkc;
-    d.xkc3 = r->tiles.xkc3; d.zirows = r->tiles.zirows; d.zirows3 = r->tiles.zirows3;
+    apply_tiles(r, r->tiles);   // tiles and the default transform of every axis
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     if (g_autotune) {
         rc = autotune_tiles(r);
@@ -931,12 +948,35 @@ int g_autotune = 1;
 int g_newton_chord = 1;   // chord steps in the FP64 Newton of new VOCE_PREC_MIXED RVEs
 int g_ir_predictor = 1;   // single-precision start of the FP64 steps in new VOCE_PREC_MIXED_IR RVEs
 
+constexpr int kMaxSchedules = 5;
+
 // schedule index k of an axis of length L (the default when out of range)
-FftPlan1 schedule_of(int L, int k)
+FftPlan1 schedule_of(int L, bool mixed, int k)
 {
-    FftPlan1 c[4];
-    const int n = fft_schedules(L, c, 4);
+    FftPlan1 c[kMaxSchedules];
+    const int n = axis_schedules(L, mixed, c, kMaxSchedules);
     return c[(k >= 0 && k < n) ? k : 0];
+}
+
+// the tiles and schedule indices an RVE descriptor runs (a restored RVE's)
+Tiles tiles_of(const RveDesc &d)
+{
+    Tiles t;
+    t.zrows = d.zrows; t.yxt = d.yxt; t.xkc = d.xkc;
+    t.xkc3 = d.xkc3; t.zirows = d.zirows; t.zirows3 = d.zirows3;
+    const FftPlan1 *pl[3] = {&d.plx, &d.ply, &d.plz};
+    int *slot[3] = {&t.sx, &t.sy, &t.sz};
+    for (int a = 0; a < 3; ++a) {
+        FftPlan1 c[kMaxSchedules];
+        const int n = axis_schedules(pl[a]->L, d.mixed, c, kMaxSchedules);
+        for (int k = 0; k < n; ++k)
+            if (c[k].n1 == pl[a]->n1 && c[k].nst == pl[a]->nst &&
+                std::memcmp(c[k].rad, pl[a]->rad, sizeof(int) * c[k].nst) == 0) {
+                *slot[a] = k;
+                break;
+            }
+    }
+    return t;
 }
 
 void apply_tiles(voce_rve *r, const Tiles &t)
@@ -945,9 +985,9 @@ void apply_tiles(voce_rve *r, const Tiles &t)
     RveDesc &d = r->d;
     d.zrows = t.zrows; d.yxt = t.yxt; d.xkc = t.xkc;
     d.xkc3 = t.xkc3; d.zirows = t.zirows; d.zirows3 = t.zirows3;
-    d.plx = schedule_of(d.nx, t.sx);
-    d.ply = schedule_of(d.ny, t.sy);
-    d.plz = schedule_of(d.nz, t.sz);
+    d.plx = schedule_of(d.nx, d.mixed, t.sx);
+    d.ply = schedule_of(d.ny, d.mixed, t.sy);
+    d.plz = schedule_of(d.nz, d.mixed, t.sz);
     r->plan_dirty = true;
 }
 
@@ -1013,9 +1053,9 @@ int autotune_tiles(voce_rve *r)
     auto time_phase = [&](const Tiles &t, int ph) -> float {
         RveDesc dt = d;
         dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc; dt.zirows = t.zirows;
-        dt.plx = schedule_of(d.nx, t.sx);
-        dt.ply = schedule_of(d.ny, t.sy);
-        dt.plz = schedule_of(d.nz, t.sz);
+        dt.plx = schedule_of(d.nx, d.mixed, t.sx);
+        dt.ply = schedule_of(d.ny, d.mixed, t.sy);
+        dt.plz = schedule_of(d.nz, d.mixed, t.sz);
         std::vector<RveDesc> one(1, dt);
         RveDesc *pd = nullptr;
         int2 *pm = nullptr;
@@ -1079,8 +1119,8 @@ int autotune_tiles(voce_rve *r)
         // every process), only the single-precision spectrum forms tune it.
         if (ph == BP_ZI || !d.mixed) continue;
         const int L = ph == BP_ZF ? d.nz : ph == BP_Y6 ? d.ny : d.nx;
-        FftPlan1 sc[4];
-        const int ns = fft_schedules(L, sc, 4);
+        FftPlan1 sc[kMaxSchedules];
+        const int ns = axis_schedules(L, true, sc, kMaxSchedules);
         int &slot = ph == BP_ZF ? best.sz : ph == BP_Y6 ? best.sy : best.sx;
         const int start = slot;
         float sched_ms = best_ms;
@@ -1547,6 +1587,7 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
     }
     r->precision = h.precision;
     r->npart = h.npart;
+    r->tiles = tiles_of(d);
     r->grain.resize((size_t)d.nv);
     r->phase.resize((size_t)d.nv);
     ok = get(r->grain.data(), sizeof(int) * (size_t)d.nv) && get(r->phase.data(), sizeof(int) * (size_t)d.nv);
@@ -1709,10 +1750,23 @@ int voce_fft_schedule_count(int L)
     return fft_schedules(L, c, 4);
 }
 
+int voce_rve_fft_schedule_count(const voce_rve *r, int axis)
+{
+    if (!r || axis < 0 || axis > 2) return -fail(VOCE_ERR_ARG, "bad argument");
+    const int L = axis == 0 ? r->d.nx : axis == 1 ? r->d.ny : r->d.nz;
+    FftPlan1 c[kMaxSchedules];
+    return axis_schedules(L, r->d.mixed, c, kMaxSchedules);
+}
+
 int voce_rve_get_fft_schedule(const voce_rve *r, int axis, int *radices, int max)
 {
     if (!r || axis < 0 || axis > 2) return -fail(VOCE_ERR_ARG, "bad argument");
     const FftPlan1 &p = axis == 0 ? r->d.plx : axis == 1 ? r->d.ply : r->d.plz;
+    if (p.n1 > 0) {   // the register FFT: its two passes
+        const int rr[2] = {p.n1, p.L / p.n1};
+        for (int k = 0; k < 2 && k < max && radices; ++k) radices[k] = rr[k];
+        return 2;
+    }
     for (int k = 0; k < p.nst && k < max && radices; ++k) radices[k] = p.rad[k];
     return p.nst;
 }
@@ -1721,8 +1775,8 @@ int voce_rve_set_fft_schedule(voce_rve *r, int axis, int k)
 {
     if (!r || axis < 0 || axis > 2) return fail(VOCE_ERR_ARG, "bad argument");
     if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch");
+    const int n = voce_rve_fft_schedule_count(r, axis);
     const int L = axis == 0 ? r->d.nx : axis == 1 ? r->d.ny : r->d.nz;
-    const int n = voce_fft_schedule_count(L);
     if (k < 0 || k >= n) return fail(VOCE_ERR_ARG, "schedule %d of %d for length %d", k, n, L);
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     Tiles t = r->tiles;
@@ -1869,6 +1923,29 @@ int voce_diag_rcp(const double *x, double *out, int n)
     if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "rcp probe: %s", cudaGetErrorString(e));
+    return VOCE_OK;
+}
+
+int voce_diag_fft(int L, int nlines, int sign, int schedule, const double *in, double *out)
+{
+    if (nlines < 1 || (sign != 1 && sign != -1) || !in || !out) return fail(VOCE_ERR_ARG, "bad argument");
+    FftPlan1 c[kMaxSchedules];
+    const int n = axis_schedules(L, true, c, kMaxSchedules);
+    if (schedule < 0 || schedule >= n) return fail(VOCE_ERR_ARG, "schedule %d of %d for length %d", schedule, n, L);
+    if ((size_t)2 * L * (nlines | 1) * sizeof(float2) > 200 * 1024)
+        return fail(VOCE_ERR_ARG, "%d lines of length %d do not fit in shared memory", nlines, L);
+    const size_t bytes = sizeof(double) * 2 * (size_t)L * nlines;
+    const auto tw = twiddles<float2, float>(L);
+    char *buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, 2 * bytes + tw.size() * sizeof(float2)));
+    double *din = reinterpret_cast<double *>(buf), *dout = reinterpret_cast<double *>(buf + bytes);
+    void *dtw = buf + 2 * bytes;
+    cudaError_t e = cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dtw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_fft_probe(c[schedule], dtw, din, dout, nlines, sign, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "fft probe: %s", cudaGetErrorString(e));
     return VOCE_OK;
 }
 

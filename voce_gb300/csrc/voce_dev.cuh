@@ -47,9 +47,13 @@ constexpr int kSysUnroll = VOCE_SYS_UNROLL;
 #define VOCE_PI_REF 3.14159265359
 #define VOCE_TWO_PI_REF 6.28318530718
 
+// One axis's transform: Stockham radix stages rad[0..nst) (n1 = 0), or, in
+// the single-precision spectrum only, the two-pass register FFT of
+// L = n1 x (L / n1) (n1 > 0; rad then keeps the default Stockham stages).
 struct FftPlan1 {
     int L, nst;
     int rad[VOCE_MAXRAD];
+    int n1;
 };
 
 // Per-RVE macro state (device, written only by the single-thread
@@ -773,12 +777,232 @@ __device__ __forceinline__ typename Cx<R>::T cmul(typename Cx<R>::T a, typename 
     return c;
 }
 
+// ---------------------------------------------------------------------------
+// Register FFT of the single-precision spectrum.  A line of length
+// L = N1 N2 runs as two passes of small DFTs held in registers (the
+// four-step Cooley-Tukey split).  Pass 1: for each t < N2, the N1 elements
+// t + N2 j are transformed over j and output k1 is multiplied by W_L^(t k1),
+// in place.  Pass 2: for each k1 < N1, those values over t are transformed
+// and X[k1 + N1 k2] is written to the other buffer.  An element crosses
+// shared memory twice (once per radix stage in the Stockham kernel below),
+// and the small DFTs -- composed the same way from radix 2, 3 and 4 -- carry
+// their twiddles as constants, with every index fixed at compile time.
+// ---------------------------------------------------------------------------
+
+// the split N1 of the lengths the register FFT runs (0: the Stockham kernel)
+__host__ __device__ inline int reg_fft_split(int L)
+{
+    switch (L) {
+    case 16: return 4;    // 4 x 4
+    case 24: return 4;    // 4 x 6
+    case 32: return 4;    // 4 x 8
+    case 48: return 6;    // 6 x 8
+    case 64: return 8;    // 8 x 8
+    case 96: return 8;    // 8 x 12
+    case 128: return 8;   // 8 x 16
+    case 192: return 12;  // 12 x 16
+    case 256: return 16;  // 16 x 16
+    default: return 0;
+    }
+}
+
+// cos(2 pi a / 48) for 0 <= a <= 12.  The small DFTs (N dividing 48) meet
+// only angles a that are multiples of 3 (N = 16) or 4 (N = 12); the values
+// are cos 0, cos pi/8 = sqrt(2 + sqrt 2) / 2, cos pi/6 = sqrt 3 / 2,
+// cos pi/4 = sqrt 2 / 2, cos pi/3, cos 3pi/8 = sqrt(2 - sqrt 2) / 2, cos pi/2.
+__host__ __device__ constexpr double cos_q48(int a)
+{
+    return a == 0 ? 1.0 : a == 3 ? 0.92387953251128675613 : a == 4 ? 0.86602540378443864676
+         : a == 6 ? 0.70710678118654752440 : a == 8 ? 0.5 : a == 9 ? 0.38268343236508977173 : 0.0;
+}
+__host__ __device__ constexpr double cos48(int a)
+{
+    a = ((a % 48) + 48) % 48;
+    return a <= 12 ? cos_q48(a) : a <= 24 ? -cos_q48(24 - a) : a <= 36 ? -cos_q48(a - 24) : cos_q48(48 - a);
+}
+__host__ __device__ constexpr double sin48(int a) { return cos48(a - 12); }
+
+template <int I> struct IC { static constexpr int v = I; };
+// f(IC<B>), f(IC<B + 1>), ..., f(IC<E - 1>)
+template <int B, int E, class F>
+__device__ __forceinline__ void sfor(F &&f)
+{
+    if constexpr (B < E) {
+        f(IC<B>{});
+        sfor<B + 1, E>(f);
+    }
+}
+
+// v W_N^E, W_N = exp(S 2 pi i / N)
+template <int N, int E, int S>
+__device__ __forceinline__ float2 rot(float2 v)
+{
+    static_assert(48 % N == 0, "small DFT lengths divide 48");
+    constexpr int a = (48 / N * E) % 48;
+    static_assert(a % 3 == 0 || a % 4 == 0, "angle without a constant");
+    if constexpr (a == 0) {
+        return v;
+    } else if constexpr (a == 24) {
+        return make_float2(-v.x, -v.y);
+    } else if constexpr (a == 12 || a == 36) {
+        // W = g i, g = +-1
+        constexpr int g = (a == 12 ? 1 : -1) * S;
+        if constexpr (g > 0) return make_float2(-v.y, v.x);
+        else return make_float2(v.y, -v.x);
+    } else {
+        constexpr float c = (float)cos48(a), s = (float)(S * sin48(a));
+        return make_float2(c * v.x - s * v.y, c * v.y + s * v.x);
+    }
+}
+
+// The small DFTs run in place on a strided view of a register array, the
+// view's element i being x[O + T i].  Output q of an N-point DFT is left in
+// view element dft_pos(N, q) (the four-step split transposes; placing the
+// outputs in the registers the inputs came from needs no temporaries, and
+// the caller indexes the permutation at compile time).
+__host__ __device__ constexpr int dft_pos(int N, int q)
+{
+    return N <= 4 ? q
+                  : dft_pos(N / (N % 4 == 0 ? 4 : 2), q / (N % 4 == 0 ? 4 : 2)) +
+                        N / (N % 4 == 0 ? 4 : 2) * dft_pos(N % 4 == 0 ? 4 : 2, q % (N % 4 == 0 ? 4 : 2));
+}
+
+// X[q] = sum_n x[n] exp(S 2 pi i n q / N) over the view, X[q] left in view
+// element dft_pos(N, q); N = A B composes radix 2, 3 and 4: A-point DFTs
+// over n = t + B j for each t, twiddles W_N^(t k), B-point DFTs over t
+template <int N, int S, int O, int T, int M>
+__device__ __forceinline__ void sdft(float2 (&x)[M])
+{
+    if constexpr (N == 2) {
+        const float2 a = x[O], b = x[O + T];
+        x[O] = make_float2(a.x + b.x, a.y + b.y);
+        x[O + T] = make_float2(a.x - b.x, a.y - b.y);
+    } else if constexpr (N == 3) {
+        constexpr float s3 = (float)(S * 0.86602540378443864676);
+        const float2 x0 = x[O], x1 = x[O + T], x2 = x[O + 2 * T];
+        const float2 u = make_float2(x1.x + x2.x, x1.y + x2.y);
+        const float2 w = make_float2(x1.x - x2.x, x1.y - x2.y);
+        const float2 m = make_float2(x0.x - 0.5f * u.x, x0.y - 0.5f * u.y);
+        x[O] = make_float2(x0.x + u.x, x0.y + u.y);
+        x[O + T] = make_float2(m.x - s3 * w.y, m.y + s3 * w.x);
+        x[O + 2 * T] = make_float2(m.x + s3 * w.y, m.y - s3 * w.x);
+    } else if constexpr (N == 4) {
+        const float2 x0 = x[O], x1 = x[O + T], x2 = x[O + 2 * T], x3 = x[O + 3 * T];
+        const float2 t0 = make_float2(x0.x + x2.x, x0.y + x2.y);
+        const float2 t1 = make_float2(x0.x - x2.x, x0.y - x2.y);
+        const float2 t2 = make_float2(x1.x + x3.x, x1.y + x3.y);
+        const float2 t3 = make_float2(x1.x - x3.x, x1.y - x3.y);
+        x[O] = make_float2(t0.x + t2.x, t0.y + t2.y);
+        x[O + 2 * T] = make_float2(t0.x - t2.x, t0.y - t2.y);
+        if constexpr (S < 0) {   // t1 -/+ i t3
+            x[O + T] = make_float2(t1.x + t3.y, t1.y - t3.x);
+            x[O + 3 * T] = make_float2(t1.x - t3.y, t1.y + t3.x);
+        } else {
+            x[O + T] = make_float2(t1.x - t3.y, t1.y + t3.x);
+            x[O + 3 * T] = make_float2(t1.x + t3.y, t1.y - t3.x);
+        }
+    } else {
+        constexpr int A = N % 4 == 0 ? 4 : 2, B = N / A;
+        sfor<0, B>([&](auto tc) { sdft<A, S, O + T * decltype(tc)::v, T * B>(x); });
+        sfor<1, B>([&](auto tc) {
+            constexpr int t = decltype(tc)::v;
+            sfor<1, A>([&](auto kc) {
+                constexpr int k = decltype(kc)::v, r = O + T * (t + B * dft_pos(A, k));
+                x[r] = rot<N, t * k, S>(x[r]);
+            });
+        });
+        sfor<0, A>([&](auto kc) { sdft<B, S, O + T * B * dft_pos(A, decltype(kc)::v), T>(x); });
+    }
+}
+
+// NL lines of length N1 N2 from a (element (l, i) at a[i * ldl + l]) into b;
+// tw[e] = exp(-2 pi i e / L) (conjugated for S = +1).  Pass 1's tasks are
+// (l, t), pass 2's (l, k1), l fastest: consecutive threads read consecutive
+// words of shared memory.
+template <int N1, int N2, int S>
+__device__ float2 *fft_reg(float2 *a, float2 *b, int NL, int ldl, const float2 *__restrict__ tw)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int dl = nthr % NL, dq = nthr / NL;
+    {
+        const int st = N2 * ldl;
+        int l = tid % NL, t = tid / NL;
+        for (int task = tid; task < NL * N2; task += nthr) {
+            float2 *p = a + t * ldl + l;
+            float2 x[N1];
+#pragma unroll
+            for (int j = 0; j < N1; ++j) x[j] = p[j * st];
+            sdft<N1, S, 0, 1>(x);
+            if (t != 0) {
+                sfor<1, N1>([&](auto kc) {
+                    constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
+                    float2 w = __ldg(tw + t * k);
+                    if (S > 0) w.y = -w.y;
+                    x[r] = cmul<float>(x[r], w);
+                });
+            }
+            sfor<0, N1>([&](auto kc) { p[decltype(kc)::v * st] = x[dft_pos(N1, decltype(kc)::v)]; });
+            l += dl;
+            t += dq;
+            if (l >= NL) { l -= NL; ++t; }
+        }
+    }
+    __syncthreads();
+    {
+        const int sb = N1 * ldl;
+        int l = tid % NL, k1 = tid / NL;
+        for (int task = tid; task < NL * N1; task += nthr) {
+            const float2 *p = a + N2 * k1 * ldl + l;
+            float2 x[N2];
+#pragma unroll
+            for (int t = 0; t < N2; ++t) x[t] = p[t * ldl];
+            sdft<N2, S, 0, 1>(x);
+            float2 *q = b + k1 * ldl + l;
+            sfor<0, N2>([&](auto kc) { q[decltype(kc)::v * sb] = x[dft_pos(N2, decltype(kc)::v)]; });
+            l += dl;
+            k1 += dq;
+            if (l >= NL) { l -= NL; ++k1; }
+        }
+    }
+    __syncthreads();
+    return b;
+}
+
+__device__ __forceinline__ float2 *fft_reg_lines(float2 *a, float2 *b, int NL, int ldl, int L,
+                                                 const float2 *__restrict__ tw, int sign)
+{
+#define VOCE_REG_FFT(L_, N1_) \
+    case L_: return sign < 0 ? fft_reg<N1_, L_ / N1_, -1>(a, b, NL, ldl, tw) : fft_reg<N1_, L_ / N1_, 1>(a, b, NL, ldl, tw);
+    switch (L) {
+    VOCE_REG_FFT(16, 4)
+    VOCE_REG_FFT(24, 4)
+    VOCE_REG_FFT(32, 4)
+    VOCE_REG_FFT(48, 6)
+    VOCE_REG_FFT(64, 8)
+    VOCE_REG_FFT(96, 8)
+    VOCE_REG_FFT(128, 8)
+    VOCE_REG_FFT(192, 12)
+    VOCE_REG_FFT(256, 16)
+    default: return nullptr;
+    }
+#undef VOCE_REG_FFT
+}
+
 template <typename R>
 __device__ typename Cx<R>::T *fft_lines(typename Cx<R>::T *a, typename Cx<R>::T *b, int NL,
                                         int ldl, const FftPlan1 &pl,
                                         const typename Cx<R>::T *__restrict__ tw, int sign)
 {
     typedef typename Cx<R>::T C;
+    if constexpr (sizeof(R) == 4) {
+        // the plan's split always matches reg_fft_split (the host sets both);
+        // an unknown length falls through to the Stockham stages, which the
+        // plan also holds
+        if (pl.n1 && reg_fft_split(pl.L) == pl.n1) {
+            C *res = fft_reg_lines(a, b, NL, ldl, pl.L, tw, sign);
+            if (res) return res;
+        }
+    }
     const int L = pl.L;
     const int tid = threadIdx.x, nthr = blockDim.x;
     int ncur = L, s = 1;

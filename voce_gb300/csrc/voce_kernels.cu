@@ -253,6 +253,37 @@ __global__ void __launch_bounds__(128) k_setup(RveDesc d, SetupConst sc, const d
 }
 
 // ---------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async): the data lands in shared
+// memory without passing through registers, so a thread can have every
+// element of its share of a tile in flight at once; cp_async_wait_all waits
+// for all of this thread's outstanding copies (a __syncthreads then makes
+// them visible to the block).  4 and 8 bytes are cached in L1 and L2, 16
+// bytes in L2 only; both addresses aligned to the size.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(__cvta_generic_to_global(gmem)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(__cvta_generic_to_global(gmem)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(__cvta_generic_to_global(gmem)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
 // FFT passes
 // ---------------------------------------------------------------------------
 // Position (a0, a1, a2) of a flat tile index i = a0 + n0 (a1 + n1 a2),
@@ -333,14 +364,33 @@ __device__ void fft_z_fwd_unit(const RveDesc &d, int rows, int unit)
     const int ytiles = ny / rows;
     const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
     const long long vb = ((long long)x * ny + y0) * nz;
-    // element (z, r, c) is sig[c][vb + r * nz + z]
-    staged_copy3<kZCopyDepth, double>(
-        6 * rows * nz, nz, rows,
-        [&](int z, int r, int c) { return __ldg(d.sig + c * nv + vb + (long long)r * nz + z); },
-        [&](int z, int r, int c, double v) {
-            C *e = &bufA[z * ldl + (c >> 1) * rows + r];
-            if (c & 1) e->y = (R)v; else e->x = (R)v;
-        });
+    if constexpr (sizeof(R) == 4) {
+        // rows y0 .. y0 + rows - 1 of a component are one run of rows * nz
+        // doubles (z fastest): the six runs are staged behind bufA by
+        // 16-byte asynchronous copies, then converted into the line layout
+        double *stage = reinterpret_cast<double *>(bufB);
+        const int run = rows * nz, half_run = run / 2;   // nz is even
+        Idx3 ic(threadIdx.x, blockDim.x, half_run, kIdxUnbounded);
+        for (int i = threadIdx.x; i < 6 * half_run; i += blockDim.x, ic.next())
+            cp_async16(stage + 2 * i, d.sig + ic.a1 * nv + vb + 2 * ic.a0);
+        cp_async_wait_all();
+        __syncthreads();
+        // element (z, r, p): components 2p and 2p + 1 of row r
+        Idx3 ix(threadIdx.x, blockDim.x, nz, rows);
+        for (int i = threadIdx.x; i < 3 * run; i += blockDim.x, ix.next()) {
+            const int z = ix.a0, r = ix.a1, p = ix.a2, q = r * nz + z;
+            bufA[z * ldl + p * rows + r] = make_float2((float)stage[2 * p * run + q], (float)stage[(2 * p + 1) * run + q]);
+        }
+    } else {
+        // element (z, r, c) is sig[c][vb + r * nz + z]
+        staged_copy3<kZCopyDepth, double>(
+            6 * rows * nz, nz, rows,
+            [&](int z, int r, int c) { return __ldg(d.sig + c * nv + vb + (long long)r * nz + z); },
+            [&](int z, int r, int c, double v) {
+                C *e = &bufA[z * ldl + (c >> 1) * rows + r];
+                if (c & 1) e->y = (R)v; else e->x = (R)v;
+            });
+    }
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plz, (const C *)d.twz, -1);
     C *spec = (C *)d.spec;
@@ -423,9 +473,16 @@ __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int 
     C *spec = (C *)specp;
     const long long base = ((long long)line * nx + x0) * ny;
     // element (y, xl) is spec[base + xl * ny + y]
-    staged_copy3<CopyDepth<R>::v, C>(
-        xt * ny, ny, kIdxUnbounded, [&](int y, int xl, int) { return spec[base + xl * ny + y]; },
-        [&](int y, int xl, int, C v) { bufA[y * ldl + xl] = v; });
+    if constexpr (sizeof(R) == 4) {
+        Idx3 il(threadIdx.x, blockDim.x, ny, kIdxUnbounded);
+        for (int i = threadIdx.x; i < xt * ny; i += blockDim.x, il.next())
+            cp_async8(&bufA[il.a0 * ldl + il.a1], spec + base + i);
+        cp_async_wait_all();
+    } else {
+        staged_copy3<CopyDepth<R>::v, C>(
+            xt * ny, ny, kIdxUnbounded, [&](int y, int xl, int) { return spec[base + xl * ny + y]; },
+            [&](int y, int xl, int, C v) { bufA[y * ldl + xl] = v; });
+    }
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.ply, (const C *)d.twy, sign);
     Idx3 ix(threadIdx.x, blockDim.x, ny, kIdxUnbounded);
@@ -450,14 +507,34 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
     // element (yl, x, c) is spec[c][kz][x][y0 + yl]
-    staged_copy3<CopyDepth<R>::v, C>(
-        6 * nx * kc, kc, nx,
-        [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
-        [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
+    if constexpr (sizeof(R) == 4) {
+        Idx3 il(threadIdx.x, blockDim.x, kc, nx);
+        for (int i = threadIdx.x; i < 6 * nx * kc; i += blockDim.x, il.next())
+            cp_async8(&bufA[il.a0 + il.a1 * ldl + il.a2 * kc],
+                      spec + il.a2 * cstride + kb + (long long)il.a1 * ny + il.a0);
+        cp_async_wait_all();
+    } else {
+        staged_copy3<CopyDepth<R>::v, C>(
+            6 * nx * kc, kc, nx,
+            [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
+            [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
+    }
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, -1);
     C *oth = (res == bufA) ? bufB : bufA;
     const int first = d.macro->first_iter;
+    // single precision: the accumulator's tile, acc[(c nx + x) kc + yl], is
+    // staged in the free line buffer while the Green loop's operands wait
+    C *acc = oth;
+    if constexpr (sizeof(R) == 4) {
+        if (!first) {
+            Idx3 il(threadIdx.x, blockDim.x, kc, nx);
+            for (int i = threadIdx.x; i < 3 * nx * kc; i += blockDim.x, il.next())
+                cp_async8(acc + i, aacc + il.a2 * cstride + kb + (long long)il.a1 * ny + il.a0);
+            cp_async_wait_all();
+            __syncthreads();
+        }
+    }
     Idx3 ig(threadIdx.x, blockDim.x, kc, kIdxUnbounded);
     for (int idx = threadIdx.x; idx < nx * kc; idx += blockDim.x, ig.next()) {
         const int yl = ig.a0, x = ig.a1;
@@ -482,7 +559,8 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
             C e;
             if (first) { e.x = ar[c]; e.y = ai[c]; }
             else {
-                e = aacc[c * cstride + o];
+                if constexpr (sizeof(R) == 4) e = acc[(c * nx + x) * kc + yl];
+                else e = aacc[c * cstride + o];
                 e.x += ar[c];
                 e.y += ai[c];
             }
@@ -513,10 +591,18 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
     C *spec = (C *)specp;
     const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
     const long long kb = (long long)kz * plane + y0;
-    staged_copy3<CopyDepth<R>::v, C>(
-        ncomp * nx * kc, kc, nx,
-        [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
-        [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
+    if constexpr (sizeof(R) == 4) {
+        Idx3 il(threadIdx.x, blockDim.x, kc, nx);
+        for (int i = threadIdx.x; i < ncomp * nx * kc; i += blockDim.x, il.next())
+            cp_async8(&bufA[il.a0 + il.a1 * ldl + il.a2 * kc],
+                      spec + il.a2 * cstride + kb + (long long)il.a1 * ny + il.a0);
+        cp_async_wait_all();
+    } else {
+        staged_copy3<CopyDepth<R>::v, C>(
+            ncomp * nx * kc, kc, nx,
+            [&](int yl, int x, int c) { return spec[c * cstride + kb + (long long)x * ny + yl]; },
+            [&](int yl, int x, int c, C v) { bufA[x * ldl + c * kc + yl] = v; });
+    }
     __syncthreads();
     C *res = fft_lines<R>(bufA, bufB, NL, ldl, d.plx, (const C *)d.twx, sign);
     Idx3 is(threadIdx.x, blockDim.x, kc, nx);
@@ -526,6 +612,88 @@ __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, i
     }
 }
 
+
+// Shared memory of the single-precision z passes, in complex floats.  The
+// forward pass stages the six stress runs (rows x nz doubles each) behind
+// its first line buffer; the inverse one (mode 0) stages the raw half-spectrum
+// columns there and the old displacement-gradient runs after both buffers.
+__host__ __device__ inline long long zf32_lines(int nz, int rows) { return (long long)nz * ((3 * rows) | 1); }
+__host__ __device__ inline long long zf32_fwd_size(int nz, int rows)
+{
+    const long long a = zf32_lines(nz, rows), st = 6LL * rows * nz;   // 6 runs of doubles
+    return a + (a > st ? a : st);
+}
+__host__ __device__ inline long long zi32_bregion(int nz, int nzh, int rows)
+{
+    const long long a = zf32_lines(nz, rows), st = 6LL * nzh * rows;
+    return a > st ? a : st;
+}
+__host__ __device__ inline long long zi32_size(int nz, int nzh, int rows)
+{
+    return zf32_lines(nz, rows) + zi32_bregion(nz, nzh, rows) + 6LL * rows * nz;   // + 6 runs of doubles
+}
+
+// Single-precision inverse z transform of the six stress-update components
+// into the symmetric displacement gradient (mode 0 of fft_z_inv_unit, with
+// the same arithmetic).  The raw columns S[(c nzh + ks) rows + r] and the
+// old gradient runs D[c rows nz + r nz + z] are staged by asynchronous
+// copies, the columns first: the block waits for them, and the gradient
+// runs arrive while the lines transform.
+__device__ void fft_z_inv_dgs_f32(const RveDesc &d, int rows, int unit)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *bufA = reinterpret_cast<float2 *>(smem_raw);
+    const int nx = d.nx, ny = d.ny, nz = d.nz, nzh = d.nzh, half = nz / 2;
+    const long long nv = d.nv;
+    const int NL = 3 * rows, ldl = NL | 1;
+    float2 *bufB = bufA + nz * ldl;
+    float2 *S = bufB;
+    double *D = reinterpret_cast<double *>(bufA + zf32_lines(nz, rows) + zi32_bregion(nz, nzh, rows));
+    const int ytiles = ny / rows;
+    const int x = unit / ytiles, y0 = (unit % ytiles) * rows;
+    const float2 *spec = (const float2 *)d.spec;
+    const long long plane = (long long)nx * ny, cstride = (long long)nzh * plane;
+    const long long xy = (long long)x * ny + y0, vb = xy * nz;
+    const int run = rows * nz, half_run = run / 2;
+    {
+        Idx3 is(threadIdx.x, blockDim.x, rows, nzh);   // (r, ks, c)
+        for (int i = threadIdx.x; i < 6 * nzh * rows; i += blockDim.x, is.next())
+            cp_async8(S + i, spec + is.a2 * cstride + (long long)is.a1 * plane + xy + is.a0);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    {
+        Idx3 ic(threadIdx.x, blockDim.x, half_run, kIdxUnbounded);
+        for (int i = threadIdx.x; i < 6 * half_run; i += blockDim.x, ic.next())
+            cp_async16(D + 2 * i, d.dgs + ic.a1 * nv + vb + 2 * ic.a0);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncthreads();
+    // element (r, k, p): line p's coefficient k of row r (components 2p, 2p + 1)
+    Idx3 ik(threadIdx.x, blockDim.x, rows, nz);
+    for (int i = threadIdx.x; i < 3 * nz * rows; i += blockDim.x, ik.next()) {
+        const int r = ik.a0, k = ik.a1, p = ik.a2;
+        const int ks = k <= half ? k : nz - k;
+        float2 A = S[(2 * p * nzh + ks) * rows + r], B = S[((2 * p + 1) * nzh + ks) * rows + r];
+        if (k == 0 || k == half) { A.y = 0.f; B.y = 0.f; }
+        if (k > half) { A.y = -A.y; B.y = -B.y; }
+        bufA[k * ldl + p * rows + r] = make_float2(A.x - B.y, A.y + B.x);
+    }
+    __syncthreads();
+    const float2 *res = fft_lines<float>(bufA, bufB, NL, ldl, d.plz, (const float2 *)d.twz, +1);
+    cp_async_wait_all();
+    __syncthreads();
+    const MacroDev *m = d.macro;
+    const double inv = d.inv_nv;
+    // element (z, r, c) is dgs[c][vb + r * nz + z] = D[i]
+    Idx3 iz(threadIdx.x, blockDim.x, nz, rows);
+    for (int i = threadIdx.x; i < 6 * run; i += blockDim.x, iz.next()) {
+        const int z = iz.a0, r = iz.a1, c = iz.a2;
+        const float2 e = res[z * ldl + (c >> 1) * rows + r];
+        const double val = (double)((c & 1) ? e.y : e.x);
+        d.dgs[(long long)c * nv + vb + (long long)r * nz + z] = D[i] + (m->ddg6[c] + val * inv);
+    }
+}
 
 // inverse z transform (Hermitian half spectrum -> real); mode 0 adds the
 // result to the symmetric displacement gradient (evolution.c:383-394),
@@ -615,19 +783,6 @@ __device__ void fft_z_inv_unit(const RveDesc &d, void *specp, int ncomp, int row
 // NR32 (the VOCE_PREC_MIXED_NR32 form): see mixed_newton below; otherwise
 // the FP64 Newton of the reference, for the FP64 and VOCE_PREC_MIXED forms.
 // ---------------------------------------------------------------------------
-
-// 4-byte asynchronous global -> shared copy (cp.async, cached in L1 and L2),
-// and the wait for all of this thread's outstanding ones
-__device__ __forceinline__ void cp_async4(float *smem, const float *gmem)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_all()
-{
-    asm volatile("cp.async.wait_all;" ::: "memory");
-}
 
 // P = S_g + S0 (packed upper triangle) of voxel v
 __device__ __forceinline__ void load_P(const RveDesc &d, long long v, double (&P)[21])
@@ -1851,8 +2006,12 @@ __global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const 
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
         if (!unit_on(d, mode == 0 ? MASK_ACTIVE : MASK_CONVERGED)) continue;
-        if (mode == 0) fft_z_inv_unit<R>(d, d.spec, 6, d.zirows, 0, e.y);
-        else fft_z_inv_unit<R>(d, d.aacc, 3, d.zirows3, 1, e.y);
+        if (mode == 0) {
+            if constexpr (sizeof(R) == 4) fft_z_inv_dgs_f32(d, d.zirows, e.y);
+            else fft_z_inv_unit<R>(d, d.spec, 6, d.zirows, 0, e.y);
+        } else {
+            fft_z_inv_unit<R>(d, d.aacc, 3, d.zirows3, 1, e.y);
+        }
         __syncthreads();
     }
 }
@@ -2003,6 +2162,10 @@ void batch_units(const RveDesc &d, int u[BP_COUNT])
 template <typename R>
 static size_t batch_smem_t(const RveDesc &d, int ph)
 {
+    if (sizeof(R) == 4) {   // the staged single-precision z passes
+        if (ph == BP_ZF) return sizeof(float2) * (size_t)zf32_fwd_size(d.nz, d.zrows);
+        if (ph == BP_ZI) return sizeof(float2) * (size_t)zi32_size(d.nz, d.nzh, d.zirows);
+    }
     switch (ph) {
     case BP_ZF: return smem_lines<R>(d.nz, 3 * d.zrows);
     case BP_Y6: case BP_Y3: return smem_lines<R>(d.ny, d.yxt);
@@ -2204,10 +2367,16 @@ int tile_candidates(const RveDesc &d, int phase, int *out, int max)
         int t = 0;
         size_t sm = 0;
         switch (phase) {
-        case BP_ZF: t = pick_div<double>(d.ny, budget / (3 * d.nz)); sm = 2 * (size_t)d.nz * ((3 * t) | 1) * cs; break;
+        case BP_ZF:
+            t = pick_div<double>(d.ny, budget / (3 * d.nz));
+            sm = f ? cs * (size_t)zf32_fwd_size(d.nz, t) : 2 * (size_t)d.nz * ((3 * t) | 1) * cs;
+            break;
         case BP_Y6: t = pick_div<double>(d.nx, budget / d.ny); sm = 2 * (size_t)d.ny * (t | 1) * cs; break;
         case BP_XG: t = pick_div<double>(d.ny, (budget * 3 / 2) / (6 * d.nx)); sm = 2 * (size_t)d.nx * ((6 * t) | 1) * cs; break;
-        case BP_ZI: t = pick_div<double>(d.ny, budget / (3 * d.nz)); sm = 2 * (size_t)d.nz * ((3 * t) | 1) * cs; break;
+        case BP_ZI:
+            t = pick_div<double>(d.ny, budget / (3 * d.nz));
+            sm = f ? cs * (size_t)zi32_size(d.nz, d.nzh, t) : 2 * (size_t)d.nz * ((3 * t) | 1) * cs;
+            break;
         default: return 0;
         }
         if (t < 1 || sm > smem_max) continue;
@@ -2370,6 +2539,41 @@ __global__ void k_rcp_probe(const double *__restrict__ x, double *__restrict__ o
 cudaError_t launch_rcp_probe(const double *x, double *out, int n, cudaStream_t s)
 {
     if (n > 0) k_rcp_probe<<<(n + 255) / 256, 256, 0, s>>>(x, out, n);
+    return cudaGetLastError();
+}
+
+// One block transforms nl lines of length pl.L with the single-precision
+// line FFT of the spectrum passes: in and out are [nl][L] complex doubles,
+// rounded to float on the way in.
+__global__ void __launch_bounds__(256) k_fft_probe(FftPlan1 pl, const float2 *__restrict__ tw,
+                                                   const double2 *__restrict__ in, double2 *__restrict__ out,
+                                                   int nl, int sign)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *a = reinterpret_cast<float2 *>(smem_raw);
+    const int L = pl.L, ldl = nl | 1;
+    float2 *b = a + L * ldl;
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
+        const int l = e / L, i = e - l * L;
+        a[i * ldl + l] = make_float2((float)in[e].x, (float)in[e].y);
+    }
+    __syncthreads();
+    const float2 *res = fft_lines<float>(a, b, nl, ldl, pl, tw, sign);
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
+        const int l = e / L, i = e - l * L;
+        const float2 v = res[i * ldl + l];
+        out[e] = make_double2(v.x, v.y);
+    }
+}
+
+cudaError_t launch_fft_probe(const FftPlan1 &pl, const void *tw, const double *in, double *out, int nl, int sign,
+                             cudaStream_t s)
+{
+    const size_t smem = (size_t)2 * pl.L * (nl | 1) * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute((const void *)k_fft_probe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fft_probe<<<1, 256, smem, s>>>(pl, (const float2 *)tw, (const double2 *)in, (double2 *)out, nl, sign);
     return cudaGetLastError();
 }
 
