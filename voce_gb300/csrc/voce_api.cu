@@ -896,6 +896,20 @@ int make_plan(const std::vector<RveDesc> &descs, int precision, RveDesc *&d_desc
             p.smem[ph] = std::max(p.smem[ph], batch_smem(descs[i], ph));
         }
     }
+    if (p.mixed) {   // the streamed y pass: all RVEs on the register FFT along y
+        long long S = 0;
+        bool all = true;
+        for (const RveDesc &d : descs) {
+            if (d.ply.n1 <= 0) all = false;
+            else S = std::max(S, (long long)d.yxt * (d.ny + d.ply.n1 + 1));
+        }
+        if (all) {
+            p.ystream = (int)((S + 1) & ~1LL);
+            const size_t sm = 2 * (size_t)p.ystream * sizeof(float2);
+            p.smem[BP_Y6] = std::max(p.smem[BP_Y6], sm);
+            p.smem[BP_Y3] = std::max(p.smem[BP_Y3], sm);
+        }
+    }
     size_t tot = 0;
     for (int ph = 0; ph < BP_COUNT; ++ph) tot += maps[ph].size();
     CUDA_TRY(cudaMalloc(&d_descs, sizeof(RveDesc) * descs.size()));

@@ -491,6 +491,51 @@ __device__ void fft_y_unit(const RveDesc &d, void *specp, int sign, int xt, int 
 }
 
 
+// ---------------------------------------------------------------------------
+// The y pass of the single-precision spectrum as a stream over a block's
+// units, for plans whose RVEs all run the register FFT along y.  A unit's
+// tile (NL = yxt lines of L = ny contiguous coefficients) is held line by
+// line at pos(l, i) = l LP + i + i / N2, LP = L + N1 + 1: pass 1 (tasks
+// (t, l), t fastest) and pass 2 (tasks (k1, l), k1 fastest) then read rows
+// of consecutive words, and pass 2 writes X[k1 + N1 k2] of line l straight
+// to the spectrum, consecutive threads to consecutive coefficients.  The
+// next unit's tile is staged by cp.async while this one transforms (two
+// tile buffers of S complex floats, S >= NL LP of every RVE of the plan).
+// ---------------------------------------------------------------------------
+template <int N1, int N2, int S>
+__device__ __forceinline__ void ystream_tile(float2 *A, int NL, float2 *g, const float2 *__restrict__ tw)
+{
+    constexpr int L = N1 * N2, LP = L + N1 + 1;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int task = tid; task < NL * N2; task += nthr) {
+        const int l = task / N2, t = task - l * N2;
+        float2 *p = A + l * LP + t;
+        float2 x[N1];
+        sfor<0, N1>([&](auto jc) { x[decltype(jc)::v] = p[(N2 + 1) * decltype(jc)::v]; });
+        sdft<N1, S, 0, 1>(x);
+        if (t != 0) {
+            sfor<1, N1>([&](auto kc) {
+                constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
+                float2 w = __ldg(tw + t * k);
+                if (S > 0) w.y = -w.y;
+                x[r] = cmul<float>(x[r], w);
+            });
+        }
+        sfor<0, N1>([&](auto kc) { p[(N2 + 1) * decltype(kc)::v] = x[dft_pos(N1, decltype(kc)::v)]; });
+    }
+    __syncthreads();
+    for (int task = tid; task < NL * N1; task += nthr) {
+        const int l = task / N1, k1 = task - l * N1;
+        const float2 *p = A + l * LP + (N2 + 1) * k1;
+        float2 x[N2];
+#pragma unroll
+        for (int t = 0; t < N2; ++t) x[t] = p[t];
+        sdft<N2, S, 0, 1>(x);
+        float2 *q = g + l * L + k1;
+        sfor<0, N2>([&](auto kc) { q[N1 * decltype(kc)::v] = x[dft_pos(N2, decltype(kc)::v)]; });
+    }
+}
+
 template <typename R>
 __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
 {
@@ -576,6 +621,144 @@ __device__ void fft_x_green_unit(const RveDesc &d, int kc, int unit)
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// The x pass with the Green operator for an RVE on the register FFT along x
+// (single precision).  The tile's NL = 6 kc lines (line l = c kc + yl:
+// component c, column y0 + yl) are held line by line at pos(l, i) = l LP +
+// i + i / N2, LP = L + N1 + 1 (odd): the forward transform runs in place on
+// A and leaves X[k] at pos(l, k) of B, the Green operator works on B, the
+// inverse transform runs in place on B and its second pass writes straight
+// to the spectrum.  Every shared-memory index inside the transforms is a
+// compile-time offset from one base per task.
+// ---------------------------------------------------------------------------
+template <int N1, int N2, int S>
+__device__ __forceinline__ void xg_pass1(float2 *A, int NL, const float2 *__restrict__ tw)
+{
+    constexpr int L = N1 * N2, LP = L + N1 + 1;
+    for (int task = threadIdx.x; task < NL * N2; task += blockDim.x) {
+        const int l = task / N2, t = task - l * N2;
+        float2 *p = A + l * LP + t;
+        float2 x[N1];
+        sfor<0, N1>([&](auto jc) { x[decltype(jc)::v] = p[(N2 + 1) * decltype(jc)::v]; });
+        sdft<N1, S, 0, 1>(x);
+        if (t != 0) {
+            sfor<1, N1>([&](auto kc) {
+                constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
+                float2 w = __ldg(tw + t * k);
+                if (S > 0) w.y = -w.y;
+                x[r] = cmul<float>(x[r], w);
+            });
+        }
+        sfor<0, N1>([&](auto kc) { p[(N2 + 1) * decltype(kc)::v] = x[dft_pos(N1, decltype(kc)::v)]; });
+    }
+}
+
+template <int N1, int N2>
+__device__ void xg_unit_f32(const RveDesc &d, int kc, int unit)
+{
+    constexpr int L = N1 * N2, LP = L + N1 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *A = reinterpret_cast<float2 *>(smem_raw);
+    const int NL = 6 * kc;
+    float2 *B = A + NL * LP;
+    const int ny = d.ny, nzh = d.nzh;
+    const int ytiles = ny / kc;
+    const int kz = unit / ytiles, y0 = (unit % ytiles) * kc;
+    float2 *spec = (float2 *)d.spec, *aacc = (float2 *)d.aacc;
+    const long long plane = (long long)L * ny, cstride = (long long)nzh * plane;
+    const long long kb = (long long)kz * plane + y0;
+    const float2 *tw = (const float2 *)d.twx;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    {   // element (yl, x, c), yl fastest
+        Idx3 il(tid, nthr, kc, L);
+        for (int i = tid; i < NL * L; i += nthr, il.next()) {
+            const int yl = il.a0, x = il.a1, c = il.a2;
+            cp_async8(A + (c * kc + yl) * LP + x + x / N2, spec + c * cstride + kb + (long long)x * ny + yl);
+        }
+        cp_async_wait_all();
+    }
+    __syncthreads();
+    xg_pass1<N1, N2, -1>(A, NL, tw);
+    __syncthreads();
+    for (int task = tid; task < NL * N1; task += nthr) {
+        const int l = task / N1, k1 = task - l * N1;
+        const float2 *p = A + l * LP + (N2 + 1) * k1;
+        float2 x[N2];
+#pragma unroll
+        for (int t = 0; t < N2; ++t) x[t] = p[t];
+        sdft<N2, -1, 0, 1>(x);
+        float2 *q = B + l * LP;
+        sfor<0, N2>([&](auto mc) {
+            const int k = k1 + N1 * decltype(mc)::v;
+            q[k + k / N2] = x[dft_pos(N2, decltype(mc)::v)];
+        });
+    }
+    __syncthreads();
+    // the accumulator's tile, acc[(c L + x) kc + yl], staged in the free A
+    const int first = d.macro->first_iter;
+    if (!first) {
+        Idx3 il(tid, nthr, kc, L);
+        for (int i = tid; i < 3 * L * kc; i += nthr, il.next())
+            cp_async8(A + i, aacc + il.a2 * cstride + kb + (long long)il.a1 * ny + il.a0);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    // the Green operator at frequency (x, y0 + yl, kz), yl fastest
+    Idx3 ig(tid, nthr, kc, kIdxUnbounded);
+    for (int idx = tid; idx < L * kc; idx += nthr, ig.next()) {
+        const int yl = ig.a0, x = ig.a1, px = x + x / N2;
+        float br[6], bi[6], ar[3], ai[3];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float2 e = B[(c * kc + yl) * LP + px];
+            br[c] = e.x;
+            bi[c] = e.y;
+        }
+        const long long o = kb + (long long)x * ny + yl;
+        green_apply<float>(d, x, y0 + yl, kz, o, br, bi, ar, ai);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) B[(c * kc + yl) * LP + px] = make_float2(br[c], bi[c]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float2 e = make_float2(ar[c], ai[c]);
+            if (!first) {
+                const float2 a = A[(c * L + x) * kc + yl];
+                e.x += a.x;
+                e.y += a.y;
+            }
+            aacc[c * cstride + o] = e;
+        }
+    }
+    __syncthreads();
+    xg_pass1<N1, N2, 1>(B, NL, tw);
+    __syncthreads();
+    // inverse pass 2: tasks (l, k1), l fastest, written to spectrum line l
+    {
+        const long long sN = (long long)N1 * ny;
+        const int dl = nthr % NL, dk = nthr / NL;
+        int l = tid % NL, k1 = tid / NL;
+        for (int task = tid; task < NL * N1; task += nthr) {
+            const float2 *p = B + l * LP + (N2 + 1) * k1;
+            float2 x[N2];
+#pragma unroll
+            for (int t = 0; t < N2; ++t) x[t] = p[t];
+            sdft<N2, 1, 0, 1>(x);
+            const int c = l / kc, yl = l - c * kc;
+            float2 *g = spec + c * cstride + kb + yl + (long long)k1 * ny;
+            sfor<0, N2>([&](auto mc) { g[decltype(mc)::v * sN] = x[dft_pos(N2, decltype(mc)::v)]; });
+            l += dl;
+            k1 += dk;
+            if (l >= NL) { l -= NL; ++k1; }
+        }
+    }
+}
+
+// smem of xg_unit_f32, bytes
+__host__ __device__ inline size_t xg32_smem(int nx, int n1, int kc)
+{
+    return 2 * sizeof(float2) * (size_t)(6 * kc) * (size_t)(nx + n1 + 1);
+}
 
 template <typename R>
 __device__ void fft_x_unit(const RveDesc &d, void *specp, int ncomp, int sign, int kc, int unit)
@@ -1959,9 +2142,93 @@ __global__ void __launch_bounds__(256) kb_fft_z_fwd(const RveDesc *descs, const 
 }
 
 // which: 0 spectrum forward, 1 spectrum inverse, 2 antisymmetric accumulator inverse
-template <typename R>
-__global__ void __launch_bounds__(256) kb_fft_y(const RveDesc *descs, const int2 *map, int total, int which)
+__device__ void fft_y_stream_f32(const RveDesc *descs, const int2 *map, int total, int which, int S)
 {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *cur = reinterpret_cast<float2 *>(smem_raw), *nxt = cur + S;
+    const int mask = which == 2 ? MASK_CONVERGED : MASK_ACTIVE;
+    const int sign = which == 0 ? -1 : +1;
+    auto next_on = [&](int w) {
+        while (w < total && !unit_on(descs[map[w].x], mask)) w += gridDim.x;
+        return w;
+    };
+    // the unit's RVE, its spectrum (y lines: contiguous) and tile base
+    auto tile = [&](int w, const RveDesc *&dp, float2 *&g) {
+        const int2 e = map[w];
+        dp = &descs[e.x];
+        const RveDesc &d = *dp;
+        const int xtiles = d.nx / d.yxt;
+        const int line = e.y / xtiles, x0 = (e.y % xtiles) * d.yxt;
+        g = (float2 *)(which == 2 ? d.aacc : d.spec) + ((long long)line * d.nx + x0) * d.ny;
+    };
+    auto issue = [&](int w, float2 *A) {
+        const RveDesc *dp;
+        float2 *g;
+        tile(w, dp, g);
+        const int L = dp->ny, N1 = dp->ply.n1, N2 = L / N1, LP = L + N1 + 1;
+        Idx3 il(threadIdx.x, blockDim.x, N2, N1);
+        for (int i = threadIdx.x; i < dp->yxt * L; i += blockDim.x, il.next())
+            cp_async8(A + il.a2 * LP + il.a0 + (N2 + 1) * il.a1, g + i);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int w = next_on(blockIdx.x);
+    if (w < total) issue(w, cur);
+    while (w < total) {
+        const int nw = next_on(w + gridDim.x);
+        if (nw < total) {
+            issue(nw, nxt);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            cp_async_wait_all();
+        }
+        __syncthreads();
+        const RveDesc *dp;
+        float2 *g;
+        tile(w, dp, g);
+        const float2 *tw = (const float2 *)dp->twy;
+        const int NL = dp->yxt;
+#define VOCE_YSTREAM(L_, N1_) \
+    case L_: \
+        if (sign < 0) ystream_tile<N1_, L_ / N1_, -1>(cur, NL, g, tw); \
+        else ystream_tile<N1_, L_ / N1_, 1>(cur, NL, g, tw); \
+        break;
+        switch (dp->ny) {
+        VOCE_YSTREAM(16, 4)
+        VOCE_YSTREAM(24, 4)
+        VOCE_YSTREAM(32, 4)
+        VOCE_YSTREAM(48, 6)
+        VOCE_YSTREAM(64, 8)
+        VOCE_YSTREAM(96, 8)
+        VOCE_YSTREAM(128, 8)
+        VOCE_YSTREAM(192, 12)
+        VOCE_YSTREAM(256, 16)
+        default: break;
+        }
+#undef VOCE_YSTREAM
+        __syncthreads();
+        float2 *t = cur; cur = nxt; nxt = t;
+        w = nw;
+    }
+}
+
+// resident blocks per SM the single-precision y and Green passes are
+// compiled for (their register budget)
+#ifndef VOCE_FFTY32_BLOCKS
+#define VOCE_FFTY32_BLOCKS 1
+#endif
+#ifndef VOCE_FFTXG32_BLOCKS
+#define VOCE_FFTXG32_BLOCKS 2
+#endif
+template <typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? VOCE_FFTY32_BLOCKS : 1)
+kb_fft_y(const RveDesc *descs, const int2 *map, int total, int which, int stream)
+{
+    if constexpr (sizeof(R) == 4) {
+        if (stream > 0) {
+            fft_y_stream_f32(descs, map, total, which, stream);
+            return;
+        }
+    }
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
@@ -1974,14 +2241,32 @@ __global__ void __launch_bounds__(256) kb_fft_y(const RveDesc *descs, const int2
 // resident blocks per SM the Green pass is compiled for (registers): 3 with
 // the FP64 spectrum (measured faster despite some spilling), 2 with FP32
 template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 8 ? 3 : 2)
+__global__ void __launch_bounds__(256, sizeof(R) == 8 ? 3 : VOCE_FFTXG32_BLOCKS)
 kb_fft_x_green(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
         const RveDesc &d = descs[e.x];
         if (!unit_on(d, MASK_ACTIVE)) continue;
-        fft_x_green_unit<R>(d, d.xkc, e.y);
+        bool done = false;
+        if constexpr (sizeof(R) == 4) {
+            if (d.plx.n1 > 0) {
+                done = true;
+                switch (d.nx) {
+                case 16: xg_unit_f32<4, 4>(d, d.xkc, e.y); break;
+                case 24: xg_unit_f32<4, 6>(d, d.xkc, e.y); break;
+                case 32: xg_unit_f32<4, 8>(d, d.xkc, e.y); break;
+                case 48: xg_unit_f32<6, 8>(d, d.xkc, e.y); break;
+                case 64: xg_unit_f32<8, 8>(d, d.xkc, e.y); break;
+                case 96: xg_unit_f32<8, 12>(d, d.xkc, e.y); break;
+                case 128: xg_unit_f32<8, 16>(d, d.xkc, e.y); break;
+                case 192: xg_unit_f32<12, 16>(d, d.xkc, e.y); break;
+                case 256: xg_unit_f32<16, 16>(d, d.xkc, e.y); break;
+                default: done = false; break;
+                }
+            }
+        }
+        if (!done) fft_x_green_unit<R>(d, d.xkc, e.y);
         __syncthreads();
     }
 }
@@ -2162,9 +2447,10 @@ void batch_units(const RveDesc &d, int u[BP_COUNT])
 template <typename R>
 static size_t batch_smem_t(const RveDesc &d, int ph)
 {
-    if (sizeof(R) == 4) {   // the staged single-precision z passes
+    if (sizeof(R) == 4) {   // the staged single-precision z passes, the register-FFT Green pass
         if (ph == BP_ZF) return sizeof(float2) * (size_t)zf32_fwd_size(d.nz, d.zrows);
         if (ph == BP_ZI) return sizeof(float2) * (size_t)zi32_size(d.nz, d.nzh, d.zirows);
+        if (ph == BP_XG && d.plx.n1 > 0) return xg32_smem(d.nx, d.plx.n1, d.xkc);
     }
     switch (ph) {
     case BP_ZF: return smem_lines<R>(d.nz, 3 * d.zrows);
@@ -2256,13 +2542,13 @@ static void plan_iteration_t(const BatchPlan &bp, cudaStream_t s, Prof &pf, cuda
     kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
     pf.end(K_FFT_Z_FWD, s);
     pf.begin(K_FFT_Y_FWD, s);
-    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0, bp.ystream);
     pf.end(K_FFT_Y_FWD, s);
     pf.begin(K_FFT_X_GREEN, s);
     kb_fft_x_green<R><<<grid_for(bp.total[BP_XG], FG), 256, bp.smem[BP_XG], s>>>(D, bp.map[BP_XG], bp.total[BP_XG]);
     pf.end(K_FFT_X_GREEN, s);
     pf.begin(K_FFT_Y_INV, s);
-    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 1);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 1, bp.ystream);
     pf.end(K_FFT_Y_INV, s);
     pf.begin(K_FFT_Z_INV, s);
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_ZI], FG), 256, bp.smem[BP_ZI], s>>>(D, bp.map[BP_ZI], bp.total[BP_ZI], 0);
@@ -2293,7 +2579,7 @@ static void plan_incr_end_t(const BatchPlan &bp, cudaStream_t s, Prof &pf)
     const RveDesc *D = bp.descs;
     pf.begin(K_INC_FFT, s);
     kb_fft_x_aacc<R><<<grid_for(bp.total[BP_X3], FG), 256, bp.smem[BP_X3], s>>>(D, bp.map[BP_X3], bp.total[BP_X3]);
-    kb_fft_y<R><<<grid_for(bp.total[BP_Y3], FG), 256, bp.smem[BP_Y3], s>>>(D, bp.map[BP_Y3], bp.total[BP_Y3], 2);
+    kb_fft_y<R><<<grid_for(bp.total[BP_Y3], FG), 256, bp.smem[BP_Y3], s>>>(D, bp.map[BP_Y3], bp.total[BP_Y3], 2, bp.ystream);
     kb_fft_z_inv<R><<<grid_for(bp.total[BP_Z3], FG), 256, bp.smem[BP_Z3], s>>>(D, bp.map[BP_Z3], bp.total[BP_Z3], 1);
     pf.end(K_INC_FFT, s, 3);
     pf.begin(K_INCR_END, s);
@@ -2336,7 +2622,7 @@ static void plan_phase_t(const BatchPlan &bp, int phase, cudaStream_t s)
         kb_fft_z_fwd<R><<<grid_for(bp.total[BP_ZF], FG), 256, bp.smem[BP_ZF], s>>>(D, bp.map[BP_ZF], bp.total[BP_ZF]);
         break;
     case BP_Y6:
-        kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0);
+        kb_fft_y<R><<<grid_for(bp.total[BP_Y6], FG), 256, bp.smem[BP_Y6], s>>>(D, bp.map[BP_Y6], bp.total[BP_Y6], 0, bp.ystream);
         break;
     case BP_XG:
         kb_fft_x_green<R><<<grid_for(bp.total[BP_XG], FG), 256, bp.smem[BP_XG], s>>>(D, bp.map[BP_XG], bp.total[BP_XG]);
@@ -2372,7 +2658,10 @@ int tile_candidates(const RveDesc &d, int phase, int *out, int max)
             sm = f ? cs * (size_t)zf32_fwd_size(d.nz, t) : 2 * (size_t)d.nz * ((3 * t) | 1) * cs;
             break;
         case BP_Y6: t = pick_div<double>(d.nx, budget / d.ny); sm = 2 * (size_t)d.ny * (t | 1) * cs; break;
-        case BP_XG: t = pick_div<double>(d.ny, (budget * 3 / 2) / (6 * d.nx)); sm = 2 * (size_t)d.nx * ((6 * t) | 1) * cs; break;
+        case BP_XG:
+            t = pick_div<double>(d.ny, (budget * 3 / 2) / (6 * d.nx));
+            sm = (f && d.plx.n1 > 0) ? xg32_smem(d.nx, d.plx.n1, t) : 2 * (size_t)d.nx * ((6 * t) | 1) * cs;
+            break;
         case BP_ZI:
             t = pick_div<double>(d.ny, budget / (3 * d.nz));
             sm = f ? cs * (size_t)zi32_size(d.nz, d.nzh, t) : 2 * (size_t)d.nz * ((3 * t) | 1) * cs;

@@ -67,6 +67,9 @@ struct BatchPlan {
     bool mixed = false;   // float spectrum
     bool nr32 = false;    // float Newton iterations (kb_nr<true>)
     bool ir = false;      // FP64-residual Newton with a float Jacobian
+    int ystream = 0;      // > 0: every RVE runs the register FFT along y; the y
+                          // pass streams its units through two tile buffers of
+                          // this many complex floats
 };
 // units of one RVE in each phase
 void batch_units(const RveDesc &d, int units[BP_COUNT]);
