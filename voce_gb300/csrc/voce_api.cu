@@ -304,16 +304,26 @@ int dalloc(voce_rve *r, T *&p, size_t count)
     return VOCE_OK;
 }
 
+// exp(-2 pi i j / L) for j < L; where the length has a register-FFT split
+// L = N1 N2, followed by the twiddle matrix of its first pass,
+// [L + k N2 + t] = exp(-2 pi i t k / L) (t < N2, k < N1): a pass-1 task
+// (t) reads its N1 twiddles at fixed offsets from one address, and the
+// threads of consecutive t read consecutive entries
 template <typename C, typename R>
 std::vector<C> twiddles(int L)
 {
-    std::vector<C> t(L);
+    const int n1 = reg_fft_split(L);
+    std::vector<C> t(n1 ? 2 * L : L);
     const long double two_pi = 6.283185307179586476925286766559005768L;
-    for (int j = 0; j < L; ++j) {
-        long double a = two_pi * (long double)j / (long double)L;
-        t[j].x = (R)cosl(a);
-        t[j].y = (R)(-sinl(a));
-    }
+    auto w = [&](long long e, C &c) {
+        const long double a = two_pi * (long double)(e % L) / (long double)L;
+        c.x = (R)cosl(a);
+        c.y = (R)(-sinl(a));
+    };
+    for (int j = 0; j < L; ++j) w(j, t[j]);
+    if (n1)
+        for (int q = 0; q < L / n1; ++q)
+            for (int k = 0; k < n1; ++k) w((long long)q * k, t[L + k * (L / n1) + q]);
     return t;
 }
 
@@ -475,12 +485,13 @@ int alloc_device(voce_rve *r)
     const int Ls[3] = {d.nx, d.ny, d.nz};
     const void **tws[3] = {&d.twx, &d.twy, &d.twz};
     for (int a = 0; a < 3; ++a) {
-        AL(p, (size_t)Ls[a] * csz);
         if (d.mixed) {
             auto t = twiddles<float2, float>(Ls[a]);
+            AL(p, t.size() * sizeof(float2));
             CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice));
         } else {
             auto t = twiddles<double2, double>(Ls[a]);
+            AL(p, t.size() * sizeof(double2));
             CUDA_TRY(cudaMemcpy(p, t.data(), t.size() * sizeof(double2), cudaMemcpyHostToDevice));
         }
         *tws[a] = p;

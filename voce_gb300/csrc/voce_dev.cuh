@@ -916,7 +916,8 @@ __device__ __forceinline__ void sdft(float2 (&x)[M])
 }
 
 // NL lines of length N1 N2 from a (element (l, i) at a[i * ldl + l]) into b;
-// tw[e] = exp(-2 pi i e / L) (conjugated for S = +1).  Pass 1's tasks are
+// tw[e] = exp(-2 pi i e / L), followed by the pass-1 twiddle matrix
+// tw[L + k N2 + t] = exp(-2 pi i t k / L) (conjugated for S = +1).  Pass 1's tasks are
 // (l, t), pass 2's (l, k1), l fastest: consecutive threads read consecutive
 // words of shared memory.
 template <int N1, int N2, int S>
@@ -934,9 +935,10 @@ __device__ float2 *fft_reg(float2 *a, float2 *b, int NL, int ldl, const float2 *
             for (int j = 0; j < N1; ++j) x[j] = p[j * st];
             sdft<N1, S, 0, 1>(x);
             if (t != 0) {
+                const float2 *wm = tw + N1 * N2 + t;   // the pass-1 twiddle matrix
                 sfor<1, N1>([&](auto kc) {
                     constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
-                    float2 w = __ldg(tw + t * k);
+                    float2 w = __ldg(wm + k * N2);
                     if (S > 0) w.y = -w.y;
                     x[r] = cmul<float>(x[r], w);
                 });

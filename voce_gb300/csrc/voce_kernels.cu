@@ -514,9 +514,10 @@ __device__ __forceinline__ void ystream_tile(float2 *A, int NL, float2 *g, const
         sfor<0, N1>([&](auto jc) { x[decltype(jc)::v] = p[(N2 + 1) * decltype(jc)::v]; });
         sdft<N1, S, 0, 1>(x);
         if (t != 0) {
+            const float2 *wm = tw + L + t;   // the pass-1 twiddle matrix
             sfor<1, N1>([&](auto kc) {
                 constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
-                float2 w = __ldg(tw + t * k);
+                float2 w = __ldg(wm + k * N2);
                 if (S > 0) w.y = -w.y;
                 x[r] = cmul<float>(x[r], w);
             });
@@ -643,9 +644,10 @@ __device__ __forceinline__ void xg_pass1(float2 *A, int NL, const float2 *__rest
         sfor<0, N1>([&](auto jc) { x[decltype(jc)::v] = p[(N2 + 1) * decltype(jc)::v]; });
         sdft<N1, S, 0, 1>(x);
         if (t != 0) {
+            const float2 *wm = tw + L + t;   // the pass-1 twiddle matrix
             sfor<1, N1>([&](auto kc) {
                 constexpr int k = decltype(kc)::v, r = dft_pos(N1, k);
-                float2 w = __ldg(tw + t * k);
+                float2 w = __ldg(wm + k * N2);
                 if (S > 0) w.y = -w.y;
                 x[r] = cmul<float>(x[r], w);
             });
@@ -2142,6 +2144,27 @@ __global__ void __launch_bounds__(256) kb_fft_z_fwd(const RveDesc *descs, const 
 }
 
 // which: 0 spectrum forward, 1 spectrum inverse, 2 antisymmetric accumulator inverse
+// cp.async of a y tile (NL lines of L contiguous coefficients at g) into the
+// stream layout; with 256 threads and L dividing 256 a thread keeps its
+// coefficient index and steps by whole lines
+template <int N1, int N2>
+__device__ __forceinline__ void ystream_issue(float2 *A, const float2 *g, int NL)
+{
+    constexpr int L = N1 * N2, LP = L + N1 + 1;
+    if (256 % L == 0 && blockDim.x == 256) {
+        constexpr int dl = 256 % L == 0 ? 256 / L : 1;
+        const int i = threadIdx.x % L;
+        float2 *s = A + (threadIdx.x / L) * LP + i + i / N2;
+        const float2 *src = g + threadIdx.x;
+        for (int l = threadIdx.x / L; l < NL; l += dl, s += dl * LP, src += 256) cp_async8(s, src);
+    } else {
+        for (int e = threadIdx.x; e < NL * L; e += blockDim.x) {
+            const int l = e / L, i = e - l * L;
+            cp_async8(A + l * LP + i + i / N2, g + e);
+        }
+    }
+}
+
 __device__ void fft_y_stream_f32(const RveDesc *descs, const int2 *map, int total, int which, int S)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -2165,10 +2188,18 @@ __device__ void fft_y_stream_f32(const RveDesc *descs, const int2 *map, int tota
         const RveDesc *dp;
         float2 *g;
         tile(w, dp, g);
-        const int L = dp->ny, N1 = dp->ply.n1, N2 = L / N1, LP = L + N1 + 1;
-        Idx3 il(threadIdx.x, blockDim.x, N2, N1);
-        for (int i = threadIdx.x; i < dp->yxt * L; i += blockDim.x, il.next())
-            cp_async8(A + il.a2 * LP + il.a0 + (N2 + 1) * il.a1, g + i);
+        switch (dp->ny) {
+        case 16: ystream_issue<4, 4>(A, g, dp->yxt); break;
+        case 24: ystream_issue<4, 6>(A, g, dp->yxt); break;
+        case 32: ystream_issue<4, 8>(A, g, dp->yxt); break;
+        case 48: ystream_issue<6, 8>(A, g, dp->yxt); break;
+        case 64: ystream_issue<8, 8>(A, g, dp->yxt); break;
+        case 96: ystream_issue<8, 12>(A, g, dp->yxt); break;
+        case 128: ystream_issue<8, 16>(A, g, dp->yxt); break;
+        case 192: ystream_issue<12, 16>(A, g, dp->yxt); break;
+        case 256: ystream_issue<16, 16>(A, g, dp->yxt); break;
+        default: break;
+        }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     int w = next_on(blockIdx.x);
@@ -2214,7 +2245,7 @@ __device__ void fft_y_stream_f32(const RveDesc *descs, const int2 *map, int tota
 // resident blocks per SM the single-precision y and Green passes are
 // compiled for (their register budget)
 #ifndef VOCE_FFTY32_BLOCKS
-#define VOCE_FFTY32_BLOCKS 1
+#define VOCE_FFTY32_BLOCKS 2
 #endif
 #ifndef VOCE_FFTXG32_BLOCKS
 #define VOCE_FFTXG32_BLOCKS 2
