@@ -1239,10 +1239,12 @@ __device__ __forceinline__ void mixed_newton(const RveDesc &d, long long v, cons
 // converge in single precision, meets a resolved-shear ratio too large for
 // |r|^n in FP32 or a non-finite value is dropped (the FP64 steps then start
 // from the Green iterate).  st is the voxel's staged column of float Schmid
-// vectors and 1/CRSS (as in the single-precision Newton form).
+// vectors and 1/CRSS (as in the single-precision Newton form).  The last
+// single-precision matrix goes to the column mout (lower triangle packed,
+// stride VOCE_NR_THREADS), where the FP64 steps read it.
 __device__ __forceinline__ bool ir_start(const RveDesc &d, long long v, const float *st,
                                          const double (&lam)[6], const double (&cc)[6], double sn2,
-                                         double (&sig)[6], int &it)
+                                         double (&sig)[6], int &it, float *mout)
 {
     float sf[6], ccf[6], Pf[21], Mf[6][6];
 #pragma unroll
@@ -1287,13 +1289,10 @@ __device__ __forceinline__ bool ir_start(const RveDesc &d, long long v, const fl
     ++it;
 #pragma unroll
     for (int c = 0; c < 6; ++c) sig[c] = (double)sf[c] - (double)x[c];
-    // the staged column is read no more: it keeps the last matrix for the
-    // FP64 steps (st is this thread's own column)
-    float *mst = const_cast<float *>(st);
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
-        for (int j = 0; j <= i; ++j) mst[sym6(i, j) * VOCE_NR_THREADS] = Mf[i][j];
+        for (int j = 0; j <= i; ++j) mout[sym6(i, j) * VOCE_NR_THREADS] = Mf[i][j];
     return true;
 }
 
@@ -1359,15 +1358,31 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
             const double it0 = __ldg(d.itau + (long long)(2 * k) * nv + v);
             const double it1 = __ldg(d.itau + (long long)(2 * k + 1) * nv + v);
             const double r = rss * (neg ? it1 : it0);
-            const double a = fabs(r);
-            const double ae = pow_abs_e(a, e);        // |r|^(n-1)
-            const double g2 = ae * r;                 // |r|^n sign(r) / gam0
+            // |r| >= 60 (or not finite), tested on the high word: an
+            // integer comparison instead of one on the FP64 pipe
+            big = big || (__double2hiint(r) & 0x7fffffff) >= 0x404E0000;
+            double g2;                                // |r|^n sign(r) / gam0
+            float aef;                                // |r|^(n-1), for the float Jacobian
+            if (e == 19) {
+                // |r|^20 = ((r^2)^2 |r|)^2)^2: five products, the sign of r
+                // put on the high word
+                const double a2 = r * r, a4 = a2 * a2, a5 = a4 * fabs(r), a10 = a5 * a5, a20 = a10 * a10;
+                g2 = __hiloint2double(__double2hiint(a20) | (__double2hiint(r) & (int)0x80000000),
+                                      __double2loint(a20));
+                if (!START) {
+                    const float af = fabsf((float)r), af2 = af * af, af4 = af2 * af2, af8 = af4 * af4;
+                    aef = af8 * af8 * af2 * af;
+                }
+            } else {
+                const double ae = pow_abs_e(fabs(r), e);   // |r|^(n-1)
+                g2 = ae * r;
+                aef = (float)ae;
+            }
 #pragma unroll
             for (int i = 0; i < 5; ++i) ed[i] = fma(sc[i], g2, ed[i]);
-            big = big || !(a < 60.0);
             if (START) continue;
             // Jacobian term gam0 n |r|^(n-1) / tau m m^T, in single precision
-            const float g1 = g1c * (float)ae * __ldg(d.itau32 + ti);
+            const float g1 = g1c * aef * __ldg(d.itau32 + ti);
             float sf[5], t[5];
 #pragma unroll
             for (int i = 0; i < 5; ++i) {
@@ -1412,13 +1427,14 @@ __device__ __forceinline__ void newton_ir(const RveDesc &d, long long v, const d
         } else {
             ir_fp64_step(d, v, sig, R);
         }
+        // the stop test of evolution.c:112 on the update itself (the
+        // reference's |sig_new - sig_old|^2 up to the rounding of one
+        // subtraction)
         double cnr = 0.0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double sn = sig[c] - R[c];
-            const double dd = sn - sig[c];
-            cnr = fma(dd, dd, cnr);
-            sig[c] = sn;
+            cnr = fma(R[c], R[c], cnr);
+            sig[c] -= R[c];
         }
         go = cnr > thr;
     }
@@ -1500,7 +1516,10 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             bool started = false;
             if (d.ir_pred) {
                 int it0 = it;
-                started = ir_start(d, v, st, lam, cc, sn2, sig, it);
+                // the staged column is read no more once the start ends: it
+                // keeps the last matrix for the FP64 steps (st is this
+                // thread's own column)
+                started = ir_start(d, v, st, lam, cc, sn2, sig, it, const_cast<float *>(st));
                 if (!started) {
 #pragma unroll
                     for (int c = 0; c < 6; ++c) sig[c] = lam[c];
