@@ -111,10 +111,12 @@ def parse():
     p.add_argument("--requests", type=int, default=200, help="cfg5: requests in the sample")
     p.add_argument("--rate", type=float, default=100.0, help="cfg5: Poisson arrival rate, req/s")
     p.add_argument("--budget-gb", type=float, default=200.0, help="cfg5: server HBM budget, GB")
-    p.add_argument("--active-voxels", type=int, default=4000000,
+    p.add_argument("--active-voxels", type=int, default=8000000,
                    help="cfg5: server active limit, voxels in flight (0: HBM budget alone)")
     p.add_argument("--served-only", action="store_true",
                    help="cfg5: serve the chosen form only (no other form, no plain FP64 server)")
+    p.add_argument("--ticks-per-round", type=int, default=16,
+                   help="cfg5: batch ticks the server runs between admissions")
     p.add_argument("--quantum", type=int, default=0,
                    help="cfg5: ticks after which a running request may be suspended (0: never)")
     p.add_argument("--inc-scale", type=float, default=0.025,
@@ -479,7 +481,8 @@ def run_voce(args, rank, world, grp):
         extras["batched"] = cfg4_core(args.extra_rves, args.increments, ("mixed_ir", "mixed_nr32"))
         extras["served"] = cfg5_core(args.extra_requests, args.extra_rate, args.extra_inc_scale,
                                      ("mixed_ir", "mixed_nr32"), plain=True, budget_gb=args.budget_gb,
-                                     active_voxels=args.active_voxels, quantum=0)
+                                     active_voxels=args.active_voxels, quantum=0,
+                                     ticks_per_round=args.ticks_per_round)
 
     if rank != 0:
         return
@@ -829,7 +832,7 @@ def run_cfg4(args):
 
 
 def cfg5_core(n_requests, rate, inc_scale, forms, plain=True, budget_gb=200.0,
-              active_voxels=4000000, quantum=0):
+              active_voxels=8000000, quantum=0, ticks_per_round=16):
     """Serving form (config 5): Poisson arrivals of RVE solve requests (edges
     U{16,32,64,128}, grains log-U[8,2048], random traceless loads,
     increments max(1, round(inc_scale x U{10..80}))), served with continuous
@@ -870,7 +873,7 @@ def cfg5_core(n_requests, rate, inc_scale, forms, plain=True, budget_gb=200.0,
                 r.close()
                 lat.append((time.perf_counter() - t0) - ta)
             return lat, vi, time.perf_counter() - t0, 0
-        with capi.Server(precision, budget, ticks_per_round=16) as s:
+        with capi.Server(precision, budget, ticks_per_round=ticks_per_round) as s:
             s.set_quantum(quantum)
             s.set_active_limit(active_voxels)
             ids = []
@@ -919,6 +922,7 @@ def cfg5_core(n_requests, rate, inc_scale, forms, plain=True, budget_gb=200.0,
                             len(reqs), rate, inc_scale),
             "requests": len(reqs), "arrival_rate_per_s": rate, "increment_scale": inc_scale,
             "hbm_budget_gb": budget_gb, "active_limit_voxels": active_voxels,
+            "ticks_per_round": ticks_per_round,
             "quantum_ticks": quantum, "request_generation_s": t_gen, "runs": out}
 
 
@@ -928,7 +932,8 @@ def run_cfg5(args):
     chosen = args.precision or "mixed_ir"
     forms = (chosen,) if args.served_only else (chosen, "mixed_nr32" if chosen != "mixed_nr32" else "mixed_ir")
     res = cfg5_core(args.requests, args.rate, args.inc_scale, forms, plain=not args.served_only,
-                    budget_gb=args.budget_gb, active_voxels=args.active_voxels, quantum=args.quantum)
+                    budget_gb=args.budget_gb, active_voxels=args.active_voxels, quantum=args.quantum,
+                    ticks_per_round=args.ticks_per_round)
     a = res["runs"]["served_" + chosen]
     line = {
         "metric": "voxel_iterations_per_s", "value": a["throughput"], "unit": "voxel-iter/s",

@@ -39,6 +39,17 @@ int voce_batch_size(const voce_batch *b);
  * still have increments to do.  Increment records of every RVE are
  * available afterwards through voce_rve_get_increment. */
 int voce_batch_run(voce_batch *b, int max_ticks, int *active_left);
+/* voce_batch_run in two halves, so that the host can work while the GPU
+ * runs the ticks (no counterpart in the reference).  voce_batch_launch
+ * enqueues up to max_ticks ticks and returns at once; voce_batch_wait waits
+ * for them and takes in the increment records, as voce_batch_run does.
+ * In between, the caller may create RVEs and add them to this batch (they
+ * join at the next launch) or do unrelated host and GPU work; it must not
+ * read or change the state of the batch's RVEs (fields, snapshots, runs).
+ * voce_batch_remove, voce_batch_run, voce_batch_launch and
+ * voce_batch_destroy wait for outstanding ticks first. */
+int voce_batch_launch(voce_batch *b, int max_ticks);
+int voce_batch_wait(voce_batch *b, int *active_left);
 /* Ticks run so far. */
 long long voce_batch_ticks(const voce_batch *b);
 /* Detaches the RVEs (they are not destroyed) and frees the batch. */

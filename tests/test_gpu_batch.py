@@ -144,3 +144,33 @@ def test_removed_mid_increment_continues_alone_or_elsewhere(voce_lib):
     _same(_snapshot(r1, 2), ref[1])
     rves[0].close()
     r1.close()
+
+
+def test_launch_wait_with_members_added_in_flight(voce_lib):
+    """voce_batch_launch / voce_batch_wait: RVEs created and added while the
+    batch's ticks run join at the next launch and give the same bits as
+    alone; so do the members that were running."""
+    prec = capi.PREC_MIXED_IR
+    cases = _cases()[:4]
+    alone = []
+    for c, n in cases:
+        with _make(c, prec) as r:
+            r.run(n)
+            alone.append(_snapshot(r, n))
+    first = [_make(c, prec) for c, _ in cases[:2]]
+    with capi.Batch(prec) as b:
+        for r, (c, n) in zip(first, cases[:2]):
+            b.add(r, n)
+        b.launch(3)
+        later = [_make(c, prec) for c, _ in cases[2:]]     # created while the ticks run
+        for r, (c, n) in zip(later, cases[2:]):
+            b.add(r, n)
+        b.wait()
+        for _ in range(10000):
+            b.launch(4)
+            if b.wait() == 0:
+                break
+        assert b.wait() == 0
+    for r, (c, n), ref in zip(first + later, cases, alone):
+        _same(_snapshot(r, n), ref)
+        r.close()

@@ -134,6 +134,8 @@ PROTOTYPES = [
     ("voce_batch_remove", C.c_int, [C.c_void_p, C.c_void_p]),
     ("voce_batch_size", C.c_int, [C.c_void_p]),
     ("voce_batch_run", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    ("voce_batch_launch", C.c_int, [C.c_void_p, C.c_int]),
+    ("voce_batch_wait", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("voce_batch_ticks", C.c_longlong, [C.c_void_p]),
     ("voce_batch_destroy", C.c_int, [C.c_void_p]),
     # voce_serve.h
@@ -534,6 +536,16 @@ class Batch:
     def run(self, max_ticks: int = 1 << 30) -> int:
         left = C.c_int()
         _check(load().voce_batch_run(self._h, max_ticks, C.byref(left)))
+        return left.value
+
+    def launch(self, max_ticks: int = 1 << 30) -> None:
+        """Enqueue up to max_ticks ticks and return (voce_batch_launch)."""
+        _check(load().voce_batch_launch(self._h, max_ticks))
+
+    def wait(self) -> int:
+        """Wait for launched ticks; RVEs with increments left (voce_batch_wait)."""
+        left = C.c_int()
+        _check(load().voce_batch_wait(self._h, C.byref(left)))
         return left.value
 
     @property

@@ -1303,6 +1303,14 @@ int ensure_ring(voce_rve *r, int cap)
 
 }  // namespace
 
+bool voce::tiles_known(const int dims[3], int precision)
+{
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    if (!g_autotune) return true;
+    if (!g_tile_file_read) read_tile_file();
+    return g_tile_cache.count(TileKey{dims[0], dims[1], dims[2], precision != VOCE_PREC_FP64 ? 1 : 0}) != 0;
+}
+
 extern "C" {
 
 int voce_rve_run(voce_rve *r, int n)
@@ -1991,6 +1999,7 @@ struct voce_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
+    bool inflight = false;   // ticks launched (voce_batch_launch) and not yet waited for
     long long ticks_total = 0;
     Prof prof;
     void drop_graph()
@@ -2119,9 +2128,15 @@ int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments)
     return VOCE_OK;
 }
 
+static int batch_finish(voce_batch *b, int *active_left);
+
 int voce_batch_remove(voce_batch *b, voce_rve *r)
 {
     if (!b || !r || r->batch != b) return fail(VOCE_ERR_ARG, "the RVE is not in this batch");
+    if (b->inflight) {
+        int rc = batch_finish(b, nullptr);
+        if (rc) return rc;
+    }
     MacroDev m;
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(cudaMemcpy(&m, r->d.macro, sizeof(m), cudaMemcpyDeviceToHost));
@@ -2139,16 +2154,20 @@ int voce_batch_remove(voce_batch *b, voce_rve *r)
 
 int voce_batch_size(const voce_batch *b) { return b ? (int)b->rves.size() : -1; }
 
-int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
+// Enqueue up to max_ticks ticks on the batch stream and return: the graph
+// (or, with profiling, the host-driven ticks, which wait for themselves)
+// and the copy of the tick counters back to pinned host memory.
+static int batch_launch(voce_batch *b, int max_ticks)
 {
-    if (!b || max_ticks < 1) return fail(VOCE_ERR_ARG, "bad argument");
     for (voce_rve *r : b->rves) CUDA_TRY(cudaStreamSynchronize(r->stream));
     if (b->dirty) {
         int rc = build_batch(b);
         if (rc) return rc;
     }
     if (b->rves.empty()) {
-        if (active_left) *active_left = 0;
+        b->h_ctl[0] = 0;
+        b->h_ctl[2] = 0;
+        b->inflight = true;
         return VOCE_OK;
     }
     b->h_ctl[0] = 0;
@@ -2168,17 +2187,53 @@ int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
     } else {
         CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
         CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-        CUDA_TRY(cudaStreamSynchronize(b->stream));
     }
+    b->inflight = true;
+    return VOCE_OK;
+}
+
+// Wait for the launched ticks and take in the increment records they made.
+static int batch_finish(voce_batch *b, int *active_left)
+{
+    if (!b->inflight) {
+        if (active_left) *active_left = b->rves.empty() ? 0 : b->h_ctl[2];
+        return VOCE_OK;
+    }
+    b->inflight = false;
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
     CUDA_TRY(cudaGetLastError());
     b->ticks_total += b->h_ctl[0];
     for (voce_rve *r : b->rves) {
+        // RVEs added after the launch have no new records yet
         int rc = collect_new(r, false);
         if (rc) return rc;
         // launches of a tick are counted per batch, not per RVE
     }
     if (active_left) *active_left = b->h_ctl[2];
     return VOCE_OK;
+}
+
+int voce_batch_launch(voce_batch *b, int max_ticks)
+{
+    if (!b || max_ticks < 1) return fail(VOCE_ERR_ARG, "bad argument");
+    if (b->inflight) {
+        int rc = batch_finish(b, nullptr);
+        if (rc) return rc;
+    }
+    return batch_launch(b, max_ticks);
+}
+
+int voce_batch_wait(voce_batch *b, int *active_left)
+{
+    if (!b) return fail(VOCE_ERR_ARG, "null argument");
+    return batch_finish(b, active_left);
+}
+
+int voce_batch_run(voce_batch *b, int max_ticks, int *active_left)
+{
+    int rc = voce_batch_launch(b, max_ticks);
+    if (rc) return rc;
+    return batch_finish(b, active_left);
 }
 
 long long voce_batch_ticks(const voce_batch *b) { return b ? b->ticks_total : -1; }
@@ -2213,6 +2268,7 @@ int voce_batch_reset_kernel_times(voce_batch *b)
 int voce_batch_destroy(voce_batch *b)
 {
     if (!b) return VOCE_OK;
+    if (b->inflight) batch_finish(b, nullptr);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (voce_rve *r : b->rves) {
         collect_new(r, false);

@@ -6,4 +6,8 @@ namespace voce {
 // Sets the message voce_last_error() returns; returns code.
 int set_error(int code, const char *msg);
 
+// Whether an RVE of this grid and precision is created without timing FFT
+// tiles (the choice is cached for the shape, or tuning is off).
+bool tiles_known(const int dims[3], int precision);
+
 }  // namespace voce

@@ -2,6 +2,7 @@
 #include "voce_batch.h"
 #include "voce_gpu.h"
 #include "voce_serve.h"
+#include "voce_internal.h"
 
 #include <algorithm>
 #include <chrono>
@@ -230,6 +231,21 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
             if (s->reqs[id]->info.t_deadline > 0.0 && now >= s->reqs[id]->info.t_deadline) late.push_back(id);
         for (long long id : late) end_request(s, *s->reqs[id], VOCE_ERR_DEADLINE);
     }
+    // the running requests' ticks go to the GPU first; admission (reading
+    // inputs, allocating and setting up new RVEs) then overlaps them, and the
+    // new requests join the batch at the next round.  A server with nothing
+    // running admits first and launches at once, and so does one whose next
+    // request is the first of its grid shape (its FFT tiles are timed on an
+    // otherwise idle GPU).
+    std::vector<long long> launched;
+    long long t0 = 0;
+    const bool tune_next = !s->queue.empty() && !voce::tiles_known(s->reqs[s->queue.front()]->info.dims, s->precision);
+    if (!s->running.empty() && !tune_next) {
+        t0 = voce_batch_ticks(s->batch);
+        int rc = voce_batch_launch(s->batch, s->ticks_per_round);
+        if (rc) return rc;
+        launched = s->running;
+    }
     // admission: first in, first out, while the footprint fits (and the
     // voxels in flight stay under the active limit, when one is set: a lone
     // request is always admitted); with a quantum, requests that have run
@@ -289,13 +305,21 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
         q.ticks_run = 0;
         s->running.push_back(q.info.id);
     }
-    if (!s->running.empty()) {
+    if (launched.empty() && !s->running.empty()) {
+        t0 = voce_batch_ticks(s->batch);
+        int rc = voce_batch_launch(s->batch, s->ticks_per_round);
+        if (rc) return rc;
+        launched = s->running;
+    }
+    if (!launched.empty()) {
         int left = 0;
-        const long long t0 = voce_batch_ticks(s->batch);
-        int rc = voce_batch_run(s->batch, s->ticks_per_round, &left);
+        int rc = voce_batch_wait(s->batch, &left);
         if (rc) return rc;
         const long long ran = voce_batch_ticks(s->batch) - t0;
-        for (long long id : s->running) s->reqs[id]->ticks_run += ran;
+        // the requests that were in the batch when it launched (one suspended
+        // meanwhile has left the running list)
+        for (long long id : launched)
+            if (s->reqs[id]->info.status == VOCE_REQ_RUNNING) s->reqs[id]->ticks_run += ran;
         std::vector<long long> still;
         for (long long id : s->running) {
             Request &q = *s->reqs[id];
