@@ -2152,8 +2152,15 @@ __device__ __forceinline__ bool unit_on(const RveDesc &d, int mask)
     return true;
 }
 
+// resident blocks per SM the single-precision z passes are compiled for
+// (256^3, mixed forms, us per launch: z forward / inverse 461 / 946 at 2,
+// 524 / 1239 at 3, 586 / 1319 at 4, 461 / 1098 at 1)
+#ifndef VOCE_FFTZ32_BLOCKS
+#define VOCE_FFTZ32_BLOCKS 2
+#endif
 template <typename R>
-__global__ void __launch_bounds__(256) kb_fft_z_fwd(const RveDesc *descs, const int2 *map, int total)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? VOCE_FFTZ32_BLOCKS : 1)
+kb_fft_z_fwd(const RveDesc *descs, const int2 *map, int total)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
@@ -2292,6 +2299,8 @@ kb_fft_y(const RveDesc *descs, const int2 *map, int total, int which, int stream
 
 // resident blocks per SM the Green pass is compiled for (registers): 3 with
 // the FP64 spectrum (measured faster despite some spilling), 2 with FP32
+// (256^3 FP32, us per launch: 641 at 2, 1095 at 3, 1227 at 4: the register
+// FFT spills below 128 registers)
 template <typename R>
 __global__ void __launch_bounds__(256, sizeof(R) == 8 ? 3 : VOCE_FFTXG32_BLOCKS)
 kb_fft_x_green(const RveDesc *descs, const int2 *map, int total)
@@ -2337,7 +2346,8 @@ __global__ void __launch_bounds__(256) kb_fft_x_aacc(const RveDesc *descs, const
 
 // mode 0: spectrum -> displacement gradient; 1: accumulator -> rotl
 template <typename R>
-__global__ void __launch_bounds__(256) kb_fft_z_inv(const RveDesc *descs, const int2 *map, int total, int mode)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? VOCE_FFTZ32_BLOCKS : 1)
+kb_fft_z_inv(const RveDesc *descs, const int2 *map, int total, int mode)
 {
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int2 e = map[w];
