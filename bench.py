@@ -245,22 +245,25 @@ def measured_peaks():
 # 262144 voxels, and the FP64 flops (FMA = 2) per Newton iteration of a voxel
 # and per voxel per launch (instruction counts fitted against the Newton
 # iterations of each launch; the capture there checks the fit).
-KB_NR_FP64_DRAM_BYTES = 269.4e6
+KB_NR_FP64_DRAM_BYTES = 268.9e6
 KB_NR_FP64_VOXELS = 262144
 KB_NR_FP64_FLOPS_PER_NEWTON = 1127
 KB_NR_FP64_FLOPS_PER_VOXEL = 307
 
 
-# The same for kb_nr<1> (mixed_nr32 form, profiles/kb_nr_nr32_cfg2_64.md); the
-# mixed form's chord-step instance of the FP64 Newton kernel moves the same
-# bytes as the FP64 one (profiles/kb_nr_mixed_cfg2_64.md: 269.1 MB).
+# The same for kb_nr<1> (mixed_nr32 form, profiles/kb_nr_nr32_cfg2_64.md) and
+# kb_nr<0, 0, 1> (mixed_ir form, profiles/kb_nr_mixed_ir_cfg2_64.md); the mixed
+# form's chord-step instance of the FP64 Newton kernel moves the same bytes as
+# the FP64 one (profiles/kb_nr_mixed_cfg2_64.md).
 KB_NR_NR32_DRAM_BYTES = 276.2e6
+KB_NR_IR_DRAM_BYTES = 539.7e6
 
 
 def profiled_traffic(precision="fp64"):
     """DRAM bytes of one Newton launch at 64^3, from the ncu capture of the
     kernel the form runs."""
-    b = KB_NR_NR32_DRAM_BYTES if precision == "mixed_nr32" else KB_NR_FP64_DRAM_BYTES
+    b = {"mixed_nr32": KB_NR_NR32_DRAM_BYTES, "mixed_ir": KB_NR_IR_DRAM_BYTES,
+         "mixed_ir_strict": KB_NR_IR_DRAM_BYTES}.get(precision, KB_NR_FP64_DRAM_BYTES)
     return b * (64 ** 3) / KB_NR_FP64_VOXELS
 
 
