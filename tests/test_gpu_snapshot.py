@@ -45,6 +45,31 @@ def test_restore_continues_bit_for_bit(prec, voce_lib):
         _same(_state(r2, range(4)), want)
 
 
+@pytest.mark.parametrize("prec", [capi.PREC_MIXED_IR, capi.PREC_FP64])
+def test_restore_in_the_middle_of_an_increment(prec, voce_lib):
+    """Taken out of a batch in the middle of an increment and restored from a
+    snapshot, an RVE finishes the increment as if it had never stopped (the
+    in-increment state: stress, displacement gradient, antisymmetric sum,
+    macro state and iteration count)."""
+    nl = _case(73)
+    with capi.Rve.from_files(nl, prec) as r:
+        r.run(2)
+        want = _state(r, range(2))
+        first = r.increment(0)["iters"]
+    assert first > 12
+    r = capi.Rve.from_files(nl, prec)
+    with capi.Batch(prec) as b:
+        b.add(r, 2)
+        b.run(first // 2)                   # stops inside the first increment
+        b.remove(r)
+    assert r.increments_done == 0
+    blob = r.snapshot()
+    r.close()
+    with capi.Rve.restore(blob) as r2:
+        r2.run(2)                           # the increment in progress counts as the first
+        _same(_state(r2, range(2)), want)
+
+
 def test_save_load_file_and_join_batch(voce_lib):
     nl = _case(72, n=12, grains=8)
     nl2 = _case(73, n=8, grains=5)
