@@ -47,7 +47,7 @@ enum {
     VOCE_ERR_PARSE = 3,       /* malformed input (mesh index mismatch: init.c:420-423) */
     VOCE_ERR_BC = 4,          /* inconsistent boundary conditions (init.c:713-735) */
     VOCE_ERR_SINGULAR = 5,    /* near-zero matrix row (kinematics.c:306-309) */
-    VOCE_ERR_UNSUPPORTED = 6, /* grid size or material this build does not handle */
+    VOCE_ERR_UNSUPPORTED = 6, /* grid size or material the library does not handle */
     VOCE_ERR_NOMEM = 7,       /* device allocation failed */
     VOCE_ERR_CUDA = 8,        /* CUDA runtime error, or no GPU */
     VOCE_ERR_STATE = 9,       /* call out of order */
