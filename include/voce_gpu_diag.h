@@ -59,6 +59,12 @@ int voce_device_memory(long long *free_bytes, long long *total_bytes);
  * outside 2^-99 <= |x| < 2^99), computed on the current device for n host
  * values: a check of that reciprocal against 1/x. */
 int voce_diag_rcp(const double *x, double *out, int n);
+/* out[i] = the square root the mixed_ir form's per-voxel error norms use (a
+ * hardware reciprocal-square-root seed refined by one Newton-Raphson step;
+ * sqrt itself outside 2^-99 <= x < 2^99), on the current device for n host
+ * values: a check of that square root against sqrt.  No counterpart in the
+ * reference. */
+int voce_diag_sqrt(const double *x, double *out, int n);
 /* The single-precision line FFT of the spectrum passes on the current
  * device: nlines lines of length L, in and out [nlines][L] complex values as
  * interleaved (re, im) doubles (rounded to float on the way in), transformed

@@ -47,3 +47,22 @@ def test_rcp_nr_within_one_ulp_inside_range_and_exact_outside(voce_lib):
     assert np.all(np.isnan(o_got[np.isnan(o_want)]))
     # the sign of zero and of infinity follows the input's
     assert np.array_equal(np.signbit(got[~np.isnan(x)]), np.signbit(x[~np.isnan(x)]))
+
+
+def test_sqrt_nr_of_the_mixed_ir_norms(voce_lib):
+    """sqrt_nr (voce_diag_sqrt): within 1e-12 relative of the correctly
+    rounded square root for 2^-99 <= x < 2^99, and sqrt itself outside
+    (zero, subnormals, far exponents, infinity, NaN, negative values)."""
+    x = _inputs()
+    got = capi.diag_sqrt(x)
+    with np.errstate(invalid="ignore"):
+        want = np.sqrt(x)
+    inside = (x >= LO) & (x < HI)
+    assert inside.sum() > 200 and (~inside).sum() > 200
+    rel = np.abs(got[inside] - want[inside]) / want[inside]
+    print("sqrt_nr max relative error", rel.max())
+    assert rel.max() <= 1e-12, (x[inside][np.argmax(rel)], rel.max())
+    o_got, o_want = got[~inside], want[~inside]
+    nan = np.isnan(o_want)
+    assert np.array_equal(o_got.view(np.uint64)[~nan], o_want.view(np.uint64)[~nan])
+    assert np.all(np.isnan(o_got[nan]))

@@ -127,6 +127,7 @@ PROTOTYPES = [
     ("voce_measure_fp64_tflops", C.c_double, []),
     ("voce_device_memory", C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     ("voce_diag_rcp", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
+    ("voce_diag_sqrt", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]),
     ("voce_diag_fft", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     # voce_batch.h
     ("voce_batch_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
@@ -261,6 +262,14 @@ def device_memory():
     f, t = C.c_longlong(), C.c_longlong()
     _check(load().voce_device_memory(C.byref(f), C.byref(t)))
     return int(f.value), int(t.value)
+
+
+def diag_sqrt(x: np.ndarray) -> np.ndarray:
+    """The mixed_ir norms' device square root (voce_diag_sqrt) of every value of x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    _check(load().voce_diag_sqrt(_dptr(x), _dptr(out), x.size))
+    return out
 
 
 def diag_rcp(x: np.ndarray) -> np.ndarray:

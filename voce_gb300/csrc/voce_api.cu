@@ -1959,6 +1959,20 @@ int voce_diag_rcp(const double *x, double *out, int n)
     return VOCE_OK;
 }
 
+int voce_diag_sqrt(const double *x, double *out, int n)
+{
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(VOCE_ERR_ARG, "bad argument");
+    if (n == 0) return VOCE_OK;
+    double *d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, sizeof(double) * 2 * (size_t)n));
+    cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_sqrt_probe(d, d + n, n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(VOCE_ERR_CUDA, "sqrt probe: %s", cudaGetErrorString(e));
+    return VOCE_OK;
+}
+
 int voce_diag_fft(int L, int nlines, int sign, int schedule, const double *in, double *out)
 {
     if (nlines < 1 || (sign != 1 && sign != -1) || !in || !out) return fail(VOCE_ERR_ARG, "bad argument");

@@ -194,6 +194,23 @@ __device__ __forceinline__ double rcp_nr(double x)
     return r;
 }
 
+// Newton-Raphson square root for the mixed_ir form's per-voxel error norms:
+// the hardware's approximate double reciprocal square root r
+// (rsqrt.approx.ftz.f64) gives y = x r, and one Heron step
+// y <- y + (x - y^2) r / 2 (the residual exact by an FMA) squares its
+// relative error, to about 1e-13; outside 2^-99 <= x < 2^99 (zero, tiny,
+// huge, negative, not finite) it falls back to sqrt.  Four FP64-pipe
+// operations instead of the correctly rounded square root's longer sequence.
+__device__ __forceinline__ double sqrt_nr(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x);
+    if (hi - 0x39C00000u >= 0x46200000u - 0x39C00000u) return sqrt(x);
+    double r;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    const double y = x * r;
+    return fma(fma(-y, y, x), 0.5 * r, y);
+}
+
 // single-precision LDL^T solve of the same system (mixed-precision Newton)
 __device__ __forceinline__ void ldlt_solve6f(const float (&M)[6][6], float (&b)[6])
 {

@@ -1569,8 +1569,10 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
                 for (int j = 0; j < 6; ++j) te = fma(-d.S0[i * 6 + j], sp[j] - lam[j], te);
                 ce = fma(te, te, ce);
             }
-            ncs = sqrt(cs);
-            nce = sqrt(ce);
+            // the mixed_ir form's norms by a Newton-Raphson square root
+            // (about 1e-13 relative); the other forms' correctly rounded
+            ncs = IR ? sqrt_nr(cs) : sqrt(cs);
+            nce = IR ? sqrt_nr(ce) : sqrt(ce);
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) { d.sig[c * nv + v] = sig[c]; d.sigp[c * nv + v] = sp[c]; }
@@ -2890,6 +2892,18 @@ __global__ void k_rcp_probe(const double *__restrict__ x, double *__restrict__ o
 cudaError_t launch_rcp_probe(const double *x, double *out, int n, cudaStream_t s)
 {
     if (n > 0) k_rcp_probe<<<(n + 255) / 256, 256, 0, s>>>(x, out, n);
+    return cudaGetLastError();
+}
+
+__global__ void k_sqrt_probe(const double *__restrict__ x, double *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = sqrt_nr(x[i]);
+}
+
+cudaError_t launch_sqrt_probe(const double *x, double *out, int n, cudaStream_t s)
+{
+    if (n > 0) k_sqrt_probe<<<(n + 255) / 256, 256, 0, s>>>(x, out, n);
     return cudaGetLastError();
 }
 

@@ -111,6 +111,7 @@ int nr_resident_blocks(int kind);
 double measure_fp64_tflops();
 // out[i] = rcp_nr(x[i]) for i < n (device arrays)
 cudaError_t launch_rcp_probe(const double *x, double *out, int n, cudaStream_t s);
+cudaError_t launch_sqrt_probe(const double *x, double *out, int n, cudaStream_t s);
 // nl lines of length pl.L through the single-precision line FFT (one block;
 // 2 L (nl | 1) complex floats of shared memory): in, out [nl][L] complex
 // doubles on the device, tw the length's float twiddles
