@@ -211,7 +211,11 @@ __device__ __forceinline__ double sqrt_nr(double x)
     return fma(fma(-y, y, x), 0.5 * r, y);
 }
 
-// single-precision LDL^T solve of the same system (mixed-precision Newton)
+// single-precision LDL^T solve of the same system (mixed-precision Newton).
+// The pivots' reciprocals are the hardware's approximate ones
+// (rcp.approx.ftz.f32, within an ulp): the solve is a Newton correction whose
+// accuracy is that of single precision anyway, and the pivots of this
+// positive definite system are normal numbers.
 __device__ __forceinline__ void ldlt_solve6f(const float (&M)[6][6], float (&b)[6])
 {
     float L[6][6], w[6][6], dinv[6];
@@ -220,7 +224,7 @@ __device__ __forceinline__ void ldlt_solve6f(const float (&M)[6][6], float (&b)[
         float dj = M[j][j];
 #pragma unroll
         for (int k = 0; k < j; ++k) dj = fmaf(-L[j][k], w[j][k], dj);
-        dinv[j] = 1.0f / dj;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(dinv[j]) : "f"(dj));
 #pragma unroll
         for (int i = j + 1; i < 6; ++i) {
             float sv = M[i][j];

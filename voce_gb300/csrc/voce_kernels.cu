@@ -1256,7 +1256,7 @@ __device__ __forceinline__ bool ir_start(const RveDesc &d, long long v, const fl
     // single precision stops at a relative update of 1e-4 (its rounding
     // floor can lie near 1e-5); the float-float step then takes the point to
     // within Newton's quadratic term of that update (~1e-9)
-    const float thr32 = (float)(1e-8 * sn2);
+    const float thr32 = 1e-8f * (float)sn2;
     const float dtf = d.dth;
     bool conv = false;
     cp_async_wait_all();   // the staged column of this voxel
