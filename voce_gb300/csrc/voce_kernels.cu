@@ -1477,6 +1477,18 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             for (int c = 0; c < 24; ++c)
                 cp_async4(st + (VOCE_STAGE_ITAU + c) * VOCE_NR_THREADS, d.itau32 + c * nv + v);
         }
+        if (IR && d.ir_pred) {
+            // the low halves the start's float-float step reads, brought to L2
+            // while its single-precision steps run: one 128-byte line per row
+            // of the warp's 32 voxels, the 105 rows shared out over the lanes
+            const int lane = tid & 31;
+            const long long vw = v - lane;
+            for (int r = lane; r < 105; r += 32) {
+                const float *b = r < 60 ? d.sch_lo + (long long)r * nv
+                               : r < 84 ? d.itau_lo + (long long)(r - 60) * nv : d.sgp_lo + (long long)(r - 84) * nv;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(b + vw));
+            }
+        }
         const int ph = d.phase[v];
         if (!d.solid[ph]) {
 #pragma unroll
