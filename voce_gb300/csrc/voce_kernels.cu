@@ -1477,10 +1477,12 @@ __device__ void nr_unit(const RveDesc &d, int unit, int nunits)
             for (int c = 0; c < 24; ++c)
                 cp_async4(st + (VOCE_STAGE_ITAU + c) * VOCE_NR_THREADS, d.itau32 + c * nv + v);
         }
-        if (IR && d.ir_pred) {
-            // the low halves the start's float-float step reads, brought to L2
-            // while its single-precision steps run: one 128-byte line per row
-            // of the warp's 32 voxels, the 105 rows shared out over the lanes
+        if ((IR && d.ir_pred) || (NR32 && polish)) {
+            // the low halves the float-float step reads (the mixed_ir start's,
+            // the mixed_nr32 acceptance step's), brought to L2 while the
+            // single-precision steps run: one 128-byte line per row of the
+            // warp's 32 voxels, the 105 rows shared out over the lanes (the
+            // FP64 rows or the next voxel's rows as well: measured slower)
             const int lane = tid & 31;
             const long long vw = v - lane;
             for (int r = lane; r < 105; r += 32) {
