@@ -255,8 +255,8 @@ KB_NR_FP64_FLOPS_PER_VOXEL = 307
 # kb_nr<0, 0, 1> (mixed_ir form, profiles/kb_nr_mixed_ir_cfg2_64.md); the mixed
 # form's chord-step instance of the FP64 Newton kernel moves the same bytes as
 # the FP64 one (profiles/kb_nr_mixed_cfg2_64.md).
-KB_NR_NR32_DRAM_BYTES = 276.2e6
-KB_NR_IR_DRAM_BYTES = 539.7e6
+KB_NR_NR32_DRAM_BYTES = 280.0e6
+KB_NR_IR_DRAM_BYTES = 545.3e6
 
 
 def profiled_traffic(precision="fp64"):
