@@ -111,11 +111,11 @@ def parse():
     p.add_argument("--requests", type=int, default=200, help="cfg5: requests in the sample")
     p.add_argument("--rate", type=float, default=100.0, help="cfg5: Poisson arrival rate, req/s")
     p.add_argument("--budget-gb", type=float, default=200.0, help="cfg5: server HBM budget, GB")
-    p.add_argument("--active-voxels", type=int, default=16000000,
+    p.add_argument("--active-voxels", type=int, default=8000000,
                    help="cfg5: server active limit, voxels in flight (0: HBM budget alone)")
     p.add_argument("--served-only", action="store_true",
                    help="cfg5: serve the chosen form only (no other form, no plain FP64 server)")
-    p.add_argument("--ticks-per-round", type=int, default=16,
+    p.add_argument("--ticks-per-round", type=int, default=8,
                    help="cfg5: batch ticks the server runs between admissions")
     p.add_argument("--quantum", type=int, default=0,
                    help="cfg5: ticks after which a running request may be suspended (0: never)")
@@ -835,7 +835,7 @@ def run_cfg4(args):
 
 
 def cfg5_core(n_requests, rate, inc_scale, forms, plain=True, budget_gb=200.0,
-              active_voxels=16000000, quantum=0, ticks_per_round=16):
+              active_voxels=8000000, quantum=0, ticks_per_round=8):
     """Serving form (config 5): Poisson arrivals of RVE solve requests (edges
     U{16,32,64,128}, grains log-U[8,2048], random traceless loads,
     increments max(1, round(inc_scale x U{10..80}))), served with continuous
