@@ -78,6 +78,39 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
+def build_sanitized(dest: str, verbose: bool = False) -> str:
+    """libvoce_gpu.so with AddressSanitizer and UndefinedBehaviorSanitizer in
+    its host code (the device code is unchanged), into directory dest; for the
+    host-side sanitizer test, which loads it with the sanitizer runtimes
+    preloaded.  Returns the library's path."""
+    os.makedirs(dest, exist_ok=True)
+    nvcc = _nvcc()
+    # one flag per -Xcompiler: nvcc splits its argument at commas
+    san = ["-g"]
+    for f in ("-fsanitize=address", "-fsanitize=undefined", "-fno-omit-frame-pointer", "-fno-sanitize-recover=all"):
+        san += ["-Xcompiler", f]
+    flags = [f for f in NVFLAGS if f != "-O3"] + ["-O1"]
+    jobs, objs = [], []
+    for src in SOURCES:
+        o = os.path.join(dest, src + ".o")
+        objs.append(o)
+        jobs.append([nvcc, *ARCH, *flags, *san, "-c", os.path.join(CSRC, src), "-o", o])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        return r
+
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(run, jobs))
+    lib = os.path.join(dest, "libvoce_gpu.so")
+    run([nvcc, *ARCH, "-shared", *san, "-o", lib, *objs, "-lcudart"])
+    return lib
+
+
 def build_legacy(verbose: bool = False, force: bool = False) -> str:
     """libvoce_legacy.so (include/voce_legacy.h): host C++ only, linked
     against libvoce_gpu.so; its undefined symbols are the reference program's
