@@ -11,7 +11,9 @@
  *     neither direction is normalised;
  *   - fftwnd_mpi(plan, 1, data, work, FFTW_NORMAL_ORDER): in-place
  *     transform, output in normal (untransposed) order;
- *   - fftwnd_mpi_local_sizes: with one rank the slab is the whole grid.
+ *   - fftwnd_mpi_local_sizes: rank r of P holds the x slab
+ *     [r nx/P, (r+1) nx/P) (one rank: the whole grid); with P > 1 the
+ *     transform runs on a shared buffer (shim_fftw.c, shim_mpi.c).
  * The transform itself is oracle/shim/fft_core.c (own mixed-radix code).
  *
  * Like FFTW 2's header this one includes <stdio.h>: evp.h:168 uses FILE

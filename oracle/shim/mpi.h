@@ -4,10 +4,12 @@
  * testf.c).  TEST INFRASTRUCTURE ONLY: it exists so that the unmodified
  * reference C sources compile and run on one core as the parity oracle.
  *
- * Semantics: one rank (rank 0, size 1).  MPI_Allreduce copies send to recv
- * and, when the environment variable VOCE_REF_TRACE names a file, appends
- * every reduced value with %.17g and a running call counter, which gives a
- * full-precision record of the reference's macro curve and error trace.
+ * Semantics: one rank by default (rank 0, size 1); VOCE_REF_RANKS=P runs P
+ * forked ranks over shared memory (shim_mpi.c).  MPI_Allreduce sums in rank
+ * order and, when the environment variable VOCE_REF_TRACE names a file,
+ * rank 0 appends every reduced value with %.17g and a running call counter,
+ * which gives a full-precision record of the reference's macro curve and
+ * error trace.
  * MPI-IO writes go to the file at the view displacement with pwrite-style
  * positioning; derived struct types keep their holes, as MPI does.
  */
@@ -65,6 +67,11 @@ int MPI_File_close(MPI_File *fh);
 /* shim-only helpers (not MPI API) */
 long shim_mpi_allreduce_calls(void);
 void shim_mpi_trace_open(const char *path);
+/* bytes of shared memory for the slab FFT's exchange buffer; call before
+ * MPI_Init (the region is mapped before the ranks fork) */
+void shim_mpi_reserve(size_t bytes);
+void *shim_mpi_shared_buffer(void);
+int shim_mpi_barrier(void);
 
 #ifdef __cplusplus
 }
