@@ -6,6 +6,7 @@
 #include "voce_io.h"
 #include "voce_kernels.h"
 #include "voce_internal.h"
+#include "voce_trace.h"
 
 #include <cuda_runtime.h>
 
@@ -559,6 +560,7 @@ long long voce_rve_footprint(const int dims[3], int precision)
 int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voce_mesh *mesh,
                     int precision, voce_rve **out)
 {
+    VOCE_TRACE("voce_rve_create");
     if (!nl || !mesh || !out || !mesh->euler_deg || !mesh->phase) return fail(VOCE_ERR_ARG, "null argument");
     *out = nullptr;
     hb_init();
@@ -1054,6 +1056,7 @@ void append_tile_file(const TileKey &k, const Tiles &t)
 
 int autotune_tiles(voce_rve *r)
 {
+    VOCE_TRACE("autotune_tiles");
     RveDesc &d = r->d;
     const TileKey key{d.nx, d.ny, d.nz, d.mixed};
     {
@@ -1315,6 +1318,7 @@ extern "C" {
 
 int voce_rve_run(voce_rve *r, int n)
 {
+    VOCE_TRACE("voce_rve_run");
     if (!r || n < 0) return fail(VOCE_ERR_ARG, "bad argument");
     if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch; run the batch or remove it");
     RveDesc &d = r->d;
@@ -1376,6 +1380,7 @@ int voce_rve_get_iter_detail(const voce_rve *r, int k, double *rows, int max)
 
 int voce_rve_get_field(voce_rve *r, int field, double *host_out)
 {
+    VOCE_TRACE("voce_rve_get_field");
     if (!r || !host_out) return fail(VOCE_ERR_ARG, "null argument");
     int per;
     switch (field) {
@@ -1581,6 +1586,7 @@ long long voce_rve_snapshot_size(voce_rve *r)
 
 int voce_rve_snapshot(voce_rve *r, void *buf, long long size)
 {
+    VOCE_TRACE("voce_rve_snapshot");
     if (!r || !buf) return fail(VOCE_ERR_ARG, "null argument");
     if (r->batch) return fail(VOCE_ERR_STATE, "the RVE belongs to a batch; remove it first");
     CUDA_TRY(cudaStreamSynchronize(r->stream));
@@ -1594,6 +1600,7 @@ int voce_rve_snapshot(voce_rve *r, void *buf, long long size)
 
 int voce_rve_restore(const void *buf, long long size, voce_rve **out)
 {
+    VOCE_TRACE("voce_rve_restore");
     if (!buf || !out) return fail(VOCE_ERR_ARG, "null argument");
     const char *in = static_cast<const char *>(buf);
     SnapHead h;
@@ -2059,6 +2066,7 @@ int set_macro_flags(voce_rve *r, int active, int target, int pending)
 // descriptor array + per-phase work lists + the tick graph
 int build_batch(voce_batch *b)
 {
+    VOCE_TRACE("build_batch");
     b->drop_plan();
     const int n = (int)b->rves.size();
     BatchPlan &p = b->plan;
@@ -2173,6 +2181,7 @@ int voce_batch_size(const voce_batch *b) { return b ? (int)b->rves.size() : -1; 
 // and the copy of the tick counters back to pinned host memory.
 static int batch_launch(voce_batch *b, int max_ticks)
 {
+    VOCE_TRACE("voce_batch_launch");
     for (voce_rve *r : b->rves) CUDA_TRY(cudaStreamSynchronize(r->stream));
     if (b->dirty) {
         int rc = build_batch(b);
@@ -2209,6 +2218,7 @@ static int batch_launch(voce_batch *b, int max_ticks)
 // Wait for the launched ticks and take in the increment records they made.
 static int batch_finish(voce_batch *b, int *active_left)
 {
+    VOCE_TRACE("voce_batch_wait");
     if (!b->inflight) {
         if (active_left) *active_left = b->rves.empty() ? 0 : b->h_ctl[2];
         return VOCE_OK;

@@ -3,6 +3,7 @@
 #include "voce_gpu.h"
 #include "voce_serve.h"
 #include "voce_internal.h"
+#include "voce_trace.h"
 
 #include <algorithm>
 #include <chrono>
@@ -219,6 +220,7 @@ int voce_server_set_deadline(voce_server *s, long long id, double t)
 
 int voce_server_poll(voce_server *s, int *running, int *queued)
 {
+    VOCE_TRACE("voce_server_poll");
     if (!s) return VOCE_ERR_ARG;
     // requests past their deadline end first (queued or running; between
     // ticks, so none of their kernels is in flight)
