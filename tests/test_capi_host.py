@@ -80,6 +80,34 @@ def test_reader_errors(voce_lib):
     assert e.value.code == 3
 
 
+def test_create_refuses_bad_inputs_before_the_gpu(voce_lib):
+    """Host-side fault injection (no GPU touched): a NaN Euler angle in the
+    mesh buffer, a singular crystal stiffness (C11 = C12, init.c:120-135 would
+    hit the LU's TINY pivot and exit(35), kinematics.c:306-309) and a phase id
+    outside the namelist's phases come back as status codes."""
+    import dataclasses
+    case = synth.small_case(4, 2, 5, n_steps=1)
+    d, nlp = _case_dir(case)
+    nl = capi.read_namelist(nlp)
+    sx = capi.read_slip(os.path.join(d, "mat.sx"))
+    eul = case.mesh.euler_deg.copy()
+    eul[7, 1] = np.nan
+    with pytest.raises(capi.VoceError) as e:
+        capi.Rve.create(nl, sx, eul, case.mesh.grain, case.mesh.phase)
+    assert e.value.code == 1 and "non-finite" in str(e.value)
+    ph = case.mesh.phase.copy()
+    ph[3] = 3
+    with pytest.raises(capi.VoceError) as e:
+        capi.Rve.create(nl, sx, case.mesh.euler_deg, case.mesh.grain, ph)
+    assert e.value.code == 3
+    bad = dataclasses.replace(case, mat=dataclasses.replace(case.mat, c12=case.mat.c11))
+    d2, nlp2 = _case_dir(bad)
+    with pytest.raises(capi.VoceError) as e:
+        capi.Rve.create(capi.read_namelist(nlp2), capi.read_slip(os.path.join(d2, "mat.sx")),
+                        bad.mesh.euler_deg, bad.mesh.grain, bad.mesh.phase)
+    assert e.value.code == 5
+
+
 def test_footprint_scales_with_grid(voce_lib):
     a = capi.footprint((64, 64, 64))
     b = capi.footprint((128, 128, 128))

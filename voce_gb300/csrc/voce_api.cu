@@ -591,6 +591,12 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     for (long long v = 0; v < nv; ++v)
         if (mesh->phase[v] < 1 || mesh->phase[v] > nl->N_phases)
             return fail(VOCE_ERR_PARSE, "phase id %d at voxel %lld", mesh->phase[v], v);
+    // a non-finite Euler angle would turn the whole field into NaN (the
+    // reference propagates it silently); refused before anything reaches
+    // the GPU
+    for (long long i = 0; i < 3 * nv; ++i)
+        if (!std::isfinite(mesh->euler_deg[i]))
+            return fail(VOCE_ERR_ARG, "non-finite Euler angle at voxel %lld", i / 3);
 
     voce_rve *r = new voce_rve();
     if (precision < VOCE_PREC_FP64 || precision > VOCE_PREC_MIXED_IR) {
