@@ -83,7 +83,15 @@ int voce_server_cancel(voce_server *s, long long id);
  * memory freed.  VOCE_ERR_STATE if it has already ended. */
 int voce_server_set_deadline(voce_server *s, long long id, double t);
 /* One round; *running and *queued receive the counts afterwards.  Expired
- * deadlines are handled first, then admission, then the batch ticks. */
+ * deadlines are handled first.  The running requests' ticks are then
+ * launched, and admission (reading inputs, creating RVEs) runs while they
+ * are on the GPU; the admitted requests join the batch at the next round.
+ * With nothing running, or when the queue head is the first request of its
+ * grid shape (its FFT tiles are timed on an idle GPU), admission comes
+ * first and the ticks are launched after it.  The round ends when the ticks
+ * are done; finished requests are retired.  A request that fails on
+ * admission, or cannot be suspended, ends with that error (VOCE_REQ_FAILED)
+ * and the other requests go on. */
 int voce_server_poll(voce_server *s, int *running, int *queued);
 double voce_server_now(const voce_server *s);
 int voce_server_info(const voce_server *s, long long id, voce_request_info *out);

@@ -268,8 +268,11 @@ int voce_server_poll(voce_server *s, int *running, int *queued)
                     if (c.ticks_run >= s->quantum && (!victim || c.ticks_run > victim->ticks_run)) victim = &c;
                 }
             if (!victim) break;
+            // a request that cannot be suspended ends with the error (its
+            // memory is freed all the same) instead of staying half out of
+            // the batch
             int rc = suspend(s, *victim);
-            if (rc) return rc;
+            if (rc) end_request(s, *victim, rc);
             continue;
         }
         s->queue.pop_front();
