@@ -19,6 +19,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -598,11 +599,12 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         if (!std::isfinite(mesh->euler_deg[i]))
             return fail(VOCE_ERR_ARG, "non-finite Euler angle at voxel %lld", i / 3);
 
-    voce_rve *r = new voce_rve();
-    if (precision < VOCE_PREC_FP64 || precision > VOCE_PREC_MIXED_IR) {
-        delete r;
+    if (precision < VOCE_PREC_FP64 || precision > VOCE_PREC_MIXED_IR)
         return fail(VOCE_ERR_ARG, "unknown precision %d", precision);
-    }
+    // owned until handed out: every early return (a failed CUDA call
+    // included) frees what was made so far
+    std::unique_ptr<voce_rve> own(new voce_rve());
+    voce_rve *r = own.get();
     r->precision = precision;
     RveDesc &d = r->d;
     SetupConst &sc = r->sc;
@@ -653,7 +655,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     {
         double s[6][6];
         std::memcpy(s, sc.cxt, sizeof(s));
-        if (!lu_inv66(s)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular crystal stiffness"); }
+        if (!lu_inv66(s)) return fail(VOCE_ERR_SINGULAR, "singular crystal stiffness");
         std::memcpy(sc.sxt, s, sizeof(s));
     }
     double tau1 = sx.tau1, thet0 = sx.thet0;
@@ -678,7 +680,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         double nb = std::sqrt(std::pow(sx.bb[s][0], 2.0) + std::pow(sx.bb[s][1], 2.0) + std::pow(sx.bb[s][2], 2.0));
         for (int q = 0; q < 3; ++q) { n[q] = sx.bn[s][q] / nn; b[q] = sx.bb[s][q] / nb; }
         double dot = n[0] * b[0] + n[1] * b[1] + n[2] * b[2];
-        if (dot > 1E-3) { delete r; return fail(VOCE_ERR_PARSE, "slip system %d is not orthogonal", s + 1); }
+        if (dot > 1E-3) return fail(VOCE_ERR_PARSE, "slip system %d is not orthogonal", s + 1);
         double a[3][3];
         for (int p = 0; p < 3; ++p)
             for (int q = 0; q < 3; ++q) a[p][q] = (n[p] * b[q] + n[q] * b[p]) / 2.0;
@@ -742,9 +744,9 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     r->npart = (int)(nb < cap ? nb : cap);
     d.npart = r->npart;
     int rc = alloc_device(r);
-    if (rc) { delete r; return rc; }
+    if (rc) return rc;
     double *d_eul = nullptr;
-    if ((rc = dalloc(r, d_eul, (size_t)(3 * nv))) != VOCE_OK) { delete r; return rc; }
+    if ((rc = dalloc(r, d_eul, (size_t)(3 * nv))) != VOCE_OK) return rc;
     CUDA_TRY(cudaMemcpyAsync(d_eul, mesh->euler_deg, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(d.phase, mesh->phase, sizeof(int) * nv, cudaMemcpyHostToDevice, r->stream));
     r->nl = *nl;
@@ -761,6 +763,12 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     std::vector<double> part((size_t)3 * r->npart * VOCE_NPART);
     CUDA_TRY(cudaMemcpyAsync(part.data(), d.part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
+    // the Euler angles live on as the orientation matrices: their staging
+    // array (24 bytes a voxel) goes now, so the RVE holds what
+    // voce_rve_footprint counts
+    r->dev_allocs.erase(std::find(r->dev_allocs.begin(), r->dev_allocs.end(), (void *)d_eul));
+    CUDA_TRY(cudaFree(d_eul));
+    d_eul = nullptr;
     // C066 = WGT * sum over voxels of C_gr (init.c:450-456), block partials
     // summed in block order
     double sums[48] = {0};
@@ -771,7 +779,7 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     double C066[6][6], S066[6][6];
     for (int q = 0; q < 36; ++q) C066[q / 6][q % 6] = sums[1 + q] * d.wgt;
     std::memcpy(S066, C066, sizeof(S066));
-    if (!lu_inv66(S066)) { delete r; return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066"); }
+    if (!lu_inv66(S066)) return fail(VOCE_ERR_SINGULAR, "singular reference stiffness C066");
     std::memcpy(d.S0, S066, sizeof(S066));
     for (int q = 0; q < 36; ++q) d.S0f[q] = (float)d.S0[q];
     if (d.nr32 || d.ir) CUDA_TRY(launch_fill_p32(d, r->stream));
@@ -824,9 +832,9 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     if (g_autotune) {
         rc = autotune_tiles(r);
-        if (rc) { delete r; return rc; }
+        if (rc) return rc;
     }
-    *out = r;
+    *out = own.release();
     return VOCE_OK;
 }
 
