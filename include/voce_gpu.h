@@ -250,7 +250,12 @@ int voce_mesh_voronoi(const int dims[3], int n_seeds, const double *seeds_xyz,
  * on the current CUDA device as a new handle that continues exactly as the
  * original would (bit-identical increments).  A snapshot is read only by the
  * same build of the library (VOCE_ERR_UNSUPPORTED otherwise); a damaged one
- * fails with VOCE_ERR_PARSE. */
+ * fails with VOCE_ERR_PARSE.  Before any of it reaches the GPU, restore
+ * checks what sizes an array or bounds an index against what creation makes
+ * for the same grid and form: the grid and spectrum sizes, the precision
+ * flags, each axis' transform schedule and FFT tiles, the work split, the
+ * slip-system count, IterMax, the phase ids and the increment and iteration
+ * counters of the macro state. */
 long long voce_rve_snapshot_size(voce_rve *r);
 int voce_rve_snapshot(voce_rve *r, void *buf, long long size);
 int voce_rve_restore(const void *buf, long long size, voce_rve **out);

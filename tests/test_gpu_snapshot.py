@@ -103,3 +103,45 @@ def test_snapshot_refused_inside_a_batch_and_damaged_blobs(voce_lib):
     with pytest.raises(capi.VoceError) as ei:
         capi.Rve.restore(blob[:-8])
     assert ei.value.code == 3
+
+
+def test_restore_refuses_edited_descriptors_and_counters(voce_lib):
+    """A snapshot whose descriptor or index-bearing state was changed is
+    refused on the host (ERR_PARSE) before anything reaches the GPU: the
+    precision, the work split, a grid edge, a phase id, the increment
+    counter.  The intact snapshot then restores and continues bit for bit.
+    The offsets follow this build's layout: a 64-byte header (macro-state
+    size at 16, precision at 28, work split at 32, total at 56), the RVE
+    descriptor from 64 (nx first), and the device state last (..., phase ids,
+    the antisymmetric sum, the macro state)."""
+    import struct
+    n = 8
+    nl = _case(75, n=n, grains=4)
+    with capi.Rve.from_files(nl, capi.PREC_FP64) as r:
+        r.run(1)
+        blob = r.snapshot()
+        r.run(1)
+        want = _state(r, range(2))
+    assert blob[:8] == b"VOCESNAP"
+    macro_size, = struct.unpack_from("<I", blob, 16)
+    total, = struct.unpack_from("<q", blob, 56)
+    assert total == len(blob)
+    assert struct.unpack_from("<iii", blob, 64) == (n, n, n)
+    nv, nspec = n ** 3, (n // 2 + 1) * n * n
+    macro_at = total - macro_size
+    phase_at = macro_at - 3 * nspec * 16 - 4 * nv
+    assert struct.unpack_from("<i", blob, phase_at)[0] in (1, 2)
+    # istep follows 119 doubles and the ints iter, iter_total of the macro state
+    istep_at = macro_at + 8 * 119 + 8
+    assert struct.unpack_from("<i", blob, istep_at)[0] >= 1
+    for at, value, what in ((28, 3, "precision"), (32, 1 << 30, "work split"),
+                            (64, 2 * n, "grid"), (phase_at, 9, "phase id"),
+                            (istep_at, 0, "counter")):
+        bad = bytearray(blob)
+        struct.pack_into("<i", bad, at, value)
+        with pytest.raises(capi.VoceError) as ei:
+            capi.Rve.restore(bytes(bad))
+        assert ei.value.code == 3 and "damaged snapshot" in str(ei.value) and what in str(ei.value), str(ei.value)
+    with capi.Rve.restore(blob) as r2:
+        r2.run(1)
+        _same(_state(r2, range(2)), want)

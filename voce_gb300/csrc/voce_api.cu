@@ -1583,6 +1583,71 @@ long long snapshot_write(voce_rve *r, char *out)
     return pos;
 }
 
+// A restored RVE runs the kernels on the descriptor its snapshot carries.
+// Everything in it that sizes an array or bounds an index is checked against
+// what creation makes for the same grid and form, so that a damaged or
+// edited snapshot is refused on the host and never reaches the GPU.  Returns
+// what is wrong, or nullptr.
+const char *snapshot_desc_problem(const SnapHead &h, const RveDesc &d, const voce_namelist &nl)
+{
+    if (h.precision < VOCE_PREC_FP64 || h.precision > VOCE_PREC_MIXED_IR) return "unknown precision";
+    if (d.mixed != (h.precision != VOCE_PREC_FP64 ? 1 : 0) ||
+        d.nr32 != (h.precision == VOCE_PREC_MIXED_NR32 ? 1 : 0) ||
+        d.ir != (h.precision == VOCE_PREC_MIXED_IR ? 1 : 0))
+        return "precision flags disagree with the precision";
+    if (d.chord < 0 || d.chord > 1 || (d.chord && h.precision != VOCE_PREC_MIXED) ||
+        d.ir_pred < 0 || d.ir_pred > 1 || (d.ir_pred && !d.ir))
+        return "Newton options disagree with the precision";
+    FftPlan1 p;
+    if (!fft_plan(d.nx, p) || !fft_plan(d.ny, p) || !fft_plan(d.nz, p) || d.nz % 2) return "unsupported grid";
+    if (d.nzh != d.nz / 2 + 1 || d.nv != (long long)d.nx * d.ny * d.nz ||
+        d.nspec != (long long)d.nzh * d.nx * d.ny || d.nv != h.nv)
+        return "grid sizes disagree";
+    // each axis runs one of its transform candidates
+    const FftPlan1 *pl[3] = {&d.plx, &d.ply, &d.plz};
+    const int L[3] = {d.nx, d.ny, d.nz};
+    for (int a = 0; a < 3; ++a) {
+        FftPlan1 c[kMaxSchedules];
+        const int n = axis_schedules(L[a], d.mixed != 0, c, kMaxSchedules);
+        bool found = false;
+        for (int k = 0; k < n && !found; ++k)
+            found = pl[a]->L == L[a] && c[k].n1 == pl[a]->n1 && c[k].nst == pl[a]->nst &&
+                    std::memcmp(c[k].rad, pl[a]->rad, sizeof(int) * c[k].nst) == 0;
+        if (!found) return "FFT schedule";
+    }
+    // the tiles: the rule voce_rve_set_tiles applies
+    const int dim[6] = {d.ny, d.nx, d.ny, d.ny, d.ny, d.ny};
+    const int tl[6] = {d.zrows, d.yxt, d.xkc, d.zirows, d.xkc3, d.zirows3};
+    for (int k = 0; k < 6; ++k)
+        if (tl[k] < 1 || dim[k] % tl[k] != 0) return "FFT tiles";
+    for (int ph = BP_ZF; ph < BP_COUNT; ++ph)
+        if (batch_smem(d, ph) > 227 * 1024) return "FFT tiles";
+    if (h.npart < 1 || d.npart != h.npart || h.npart > std::max<long long>(1, (d.nv + 127) / 128))
+        return "work split";
+    if (d.nsys < 1 || d.nsys > VOCE_NS) return "number of slip systems";
+    if (d.iter_max < 0 || d.iter_max != nl.IterMax) return "IterMax";
+    if (d.ipow_n != -1 && (d.ipow_n < 1 || d.ipow_n > 256)) return "flow exponent";
+    return nullptr;
+}
+
+// The device state bytes the kernels index by: phase ids (1 or 2) and the
+// macro state's increment and iteration counters.
+const char *snapshot_state_problem(const RveDesc &d, void **which, const char *bytes, size_t n)
+{
+    if (which == (void **)&d.phase) {
+        for (size_t i = 0; i < n / sizeof(int); ++i) {
+            int v;
+            std::memcpy(&v, bytes + i * sizeof(int), sizeof(int));
+            if (v < 1 || v > 2) return "phase id";
+        }
+    } else if (which == (void **)&d.macro) {
+        MacroDev m;
+        std::memcpy(&m, bytes, sizeof(m));
+        if (m.istep < 1 || m.iter < 0 || m.iter > d.iter_max) return "increment or iteration counter";
+    }
+    return nullptr;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1639,6 +1704,10 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
         delete r;
         return fail(VOCE_ERR_PARSE, "snapshot header and descriptor disagree");
     }
+    if (const char *bad = snapshot_desc_problem(h, d, r->nl)) {
+        delete r;
+        return fail(VOCE_ERR_PARSE, "damaged snapshot: %s", bad);
+    }
     r->precision = h.precision;
     r->npart = h.npart;
     r->tiles = tiles_of(d);
@@ -1674,6 +1743,10 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
     for_state(d, [&](void **p, size_t n) {
         if (rc) return;
         if (pos + (long long)n > size) { rc = fail(VOCE_ERR_PARSE, "truncated snapshot"); return; }
+        if (const char *bad = snapshot_state_problem(d, p, in + pos, n)) {
+            rc = fail(VOCE_ERR_PARSE, "damaged snapshot: %s", bad);
+            return;
+        }
         cudaError_t e2 = cudaMemcpy(*p, in + pos, n, cudaMemcpyHostToDevice);
         if (e2 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore copy: %s", cudaGetErrorString(e2));
         pos += (long long)n;
