@@ -245,8 +245,8 @@ int voce_mesh_voronoi(const int dims[3], int n_seeds, const double *seeds_xyz,
 /* Snapshot / restore (no counterpart in the reference, which has no resume:
  * its io.c dumps are write-only).  A snapshot holds everything an RVE
  * carries from one call to the next: the per-voxel fields, hardening and
- * orientation state, the macro state, the increment records and the
- * namelist.  Taken between calls (not while the RVE is in a batch); restored
+ * orientation state, the macro state, the increment records, the
+ * per-iteration log rows of an increment in progress and the namelist.  Taken between calls (not while the RVE is in a batch); restored
  * on the current CUDA device as a new handle that continues exactly as the
  * original would (bit-identical increments).  A snapshot is read only by the
  * same build of the library (VOCE_ERR_UNSUPPORTED otherwise); a damaged one

@@ -19,14 +19,19 @@ def _case(seed, n=16, grains=12):
 
 
 def _state(r, ks):
-    return ([r.increment(k) for k in ks], r.field("sig_voigt"), r.field("edot_voigt"),
-            r.field("crss"), r.field("tranmat"), r.field("disgrad"), r.field("gammatotal"))
+    return ([r.increment(k) for k in ks], [r.iter_detail(k) for k in ks],
+            r.field("sig_voigt"), r.field("edot_voigt"), r.field("crss"), r.field("tranmat"),
+            r.field("disgrad"), r.field("gammatotal"))
 
 
 def _same(a, b):
-    ia, *fa = a
-    ib, *fb = b
+    ia, la, *fa = a
+    ib, lb, *fb = b
     assert ia == ib
+    # the per-iteration log (err.out's lines) of every increment
+    assert len(la) == len(lb)
+    for x, y in zip(la, lb):
+        assert np.array_equal(x, y)
     for x, y in zip(fa, fb):
         assert np.array_equal(x, y)
 
@@ -128,7 +133,8 @@ def test_restore_refuses_edited_descriptors_and_counters(voce_lib):
     assert total == len(blob)
     assert struct.unpack_from("<iii", blob, 64) == (n, n, n)
     nv, nspec = n ** 3, (n // 2 + 1) * n * n
-    macro_at = total - macro_size
+    # last: the log rows of the increment in progress, 12 doubles an iteration
+    macro_at = total - 12 * 8 * capi.read_namelist(nl).IterMax - macro_size
     phase_at = macro_at - 3 * nspec * 16 - 4 * nv
     assert struct.unpack_from("<i", blob, phase_at)[0] in (1, 2)
     # istep follows 119 doubles and the ints iter, iter_total of the macro state
@@ -145,3 +151,34 @@ def test_restore_refuses_edited_descriptors_and_counters(voce_lib):
     with capi.Rve.restore(blob) as r2:
         r2.run(1)
         _same(_state(r2, range(2)), want)
+
+
+def test_batch_growing_the_record_ring_in_the_middle_of_an_increment(voce_lib):
+    """An RVE taken out of a batch in the middle of an increment and added
+    again for more increments than its record ring holds (the ring grows)
+    keeps the log rows of the iterations it has run: the increment's record
+    and err.out lines equal those of an uninterrupted run."""
+    nl = _case(76, n=8, grains=4)
+    with capi.Rve.from_files(nl) as r:
+        r.run(1)
+        want = _state(r, range(1))
+        first = r.increment(0)["iters"]
+    assert first > 12
+    with capi.Rve.from_files(nl) as r:
+        with capi.Batch(capi.PREC_FP64) as b:
+            b.add(r, 1)
+            b.run(first // 2)               # stops inside the first increment
+            b.remove(r)
+            assert r.increments_done == 0
+            b.add(r, 40)                    # more than the 32 records the ring starts with
+            for _ in range(first):
+                if r.increments_done >= 1:
+                    break
+                b.run(8)
+            assert r.increments_done >= 1
+            b.remove(r)
+        got = _state(r, range(1))
+    # the fields have moved on into the next increment; the record and the log
+    # of the first increment are compared
+    assert got[0] == want[0]
+    assert len(got[1]) == 1 and np.array_equal(got[1][0], want[1][0])

@@ -1309,6 +1309,27 @@ int ensure_ring(voce_rve *r, int cap)
     for (int k = 0; k < d.incr_cap; ++k)
         if (old[k].istep > 0)
             CUDA_TRY(cudaMemcpy(ic + (old[k].istep - 1) % cap, &old[k], sizeof(IncrDev), cudaMemcpyHostToDevice));
+    // the increment in progress keeps the log rows of its iterations so far
+    // (an RVE taken out of a batch in the middle of an increment)
+    if (d.iter_max > 0) {
+        MacroDev m;
+        CUDA_TRY(cudaMemcpy(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost));
+        if (m.istep >= 1) {
+            const size_t rows = (size_t)d.iter_max * VOCE_ITLOG;
+            CUDA_TRY(cudaMemcpy(lg + (size_t)((m.istep - 1) % cap) * rows,
+                                d.itlog + (size_t)((m.istep - 1) % d.incr_cap) * rows, sizeof(double) * rows,
+                                cudaMemcpyDeviceToDevice));
+        }
+    }
+    // the old ring goes (nothing in flight uses it: the RVE's stream was
+    // drained by collect_new, and it belongs to no batch)
+    for (void *q : {(void *)d.itlog, (void *)d.incr}) {
+        auto it = std::find(r->dev_allocs.begin(), r->dev_allocs.end(), q);
+        if (it != r->dev_allocs.end()) {
+            r->dev_allocs.erase(it);
+            CUDA_TRY(cudaFree(q));
+        }
+    }
     d.itlog = lg;
     d.incr = ic;
     d.incr_cap = cap;
@@ -1547,7 +1568,7 @@ long long snapshot_write(voce_rve *r, char *out)
     SnapHead h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, kSnapMagic, 8);
-    h.version = 2;
+    h.version = 3;
     h.desc_size = sizeof(RveDesc);
     h.macro_size = sizeof(MacroDev);
     h.nl_size = sizeof(voce_namelist);
@@ -1575,6 +1596,20 @@ long long snapshot_write(voce_rve *r, char *out)
         }
         pos += (long long)n;
     });
+    // the log rows of the increment in progress (its iterations so far; the
+    // records of finished increments are above)
+    if (d.iter_max > 0) {
+        const size_t rows = (size_t)d.iter_max * VOCE_ITLOG;
+        if (out && rc == VOCE_OK) {
+            MacroDev m;
+            cudaError_t e = cudaMemcpy(&m, d.macro, sizeof(m), cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(out + pos, d.itlog + (size_t)((m.istep - 1) % d.incr_cap) * rows,
+                               sizeof(double) * rows, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "snapshot copy: %s", cudaGetErrorString(e));
+        }
+        pos += (long long)(sizeof(double) * rows);
+    }
     if (rc) return -rc;
     if (out) {
         h.total = pos;
@@ -1686,7 +1721,7 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
     if (size < (long long)sizeof(h)) return fail(VOCE_ERR_PARSE, "snapshot too short");
     std::memcpy(&h, in, sizeof(h));
     if (std::memcmp(h.magic, kSnapMagic, 8) != 0) return fail(VOCE_ERR_PARSE, "not an RVE snapshot");
-    if (h.version != 2 || h.desc_size != sizeof(RveDesc) || h.macro_size != sizeof(MacroDev) ||
+    if (h.version != 3 || h.desc_size != sizeof(RveDesc) || h.macro_size != sizeof(MacroDev) ||
         h.nl_size != sizeof(voce_namelist) || h.incr_size != sizeof(voce_increment))
         return fail(VOCE_ERR_UNSUPPORTED, "snapshot written by a different build of the library");
     if (h.total != size) return fail(VOCE_ERR_PARSE, "snapshot of %lld bytes, header says %lld", size, (long long)h.total);
@@ -1740,6 +1775,7 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
         delete r;
         return rc;
     }
+    int istep = 1;
     for_state(d, [&](void **p, size_t n) {
         if (rc) return;
         if (pos + (long long)n > size) { rc = fail(VOCE_ERR_PARSE, "truncated snapshot"); return; }
@@ -1747,10 +1783,28 @@ int voce_rve_restore(const void *buf, long long size, voce_rve **out)
             rc = fail(VOCE_ERR_PARSE, "damaged snapshot: %s", bad);
             return;
         }
+        if (p == (void **)&d.macro) {
+            MacroDev m;
+            std::memcpy(&m, in + pos, sizeof(m));
+            istep = m.istep;
+        }
         cudaError_t e2 = cudaMemcpy(*p, in + pos, n, cudaMemcpyHostToDevice);
         if (e2 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore copy: %s", cudaGetErrorString(e2));
         pos += (long long)n;
     });
+    // the log rows of the increment in progress, into its slot of the new ring
+    if (rc == VOCE_OK && d.iter_max > 0) {
+        const size_t rows = (size_t)d.iter_max * VOCE_ITLOG;
+        if (pos + (long long)(sizeof(double) * rows) > size) {
+            rc = fail(VOCE_ERR_PARSE, "truncated snapshot");
+        } else {
+            cudaError_t e4 = cudaMemcpy(d.itlog + (size_t)((istep - 1) % d.incr_cap) * rows, in + pos,
+                                        sizeof(double) * rows, cudaMemcpyHostToDevice);
+            if (e4 != cudaSuccess) rc = fail(VOCE_ERR_CUDA, "restore copy: %s", cudaGetErrorString(e4));
+            pos += (long long)(sizeof(double) * rows);
+        }
+    }
+    if (rc == VOCE_OK && pos != size) rc = fail(VOCE_ERR_PARSE, "snapshot of %lld bytes, %lld read", size, pos);
     if (rc == VOCE_OK) {
         cudaError_t e3 = launch_fill_green(d, r->stream);
         if (e3 == cudaSuccess) e3 = cudaStreamSynchronize(r->stream);
@@ -2218,7 +2272,7 @@ int voce_batch_create(int precision, voce_batch **out)
 
 int voce_batch_add(voce_batch *b, voce_rve *r, int n_increments)
 {
-    if (!b || !r || n_increments < 1) return fail(VOCE_ERR_ARG, "bad argument");
+    if (!b || !r || n_increments < 1 || n_increments > (1 << 24)) return fail(VOCE_ERR_ARG, "bad argument");
     if (r->batch) return fail(VOCE_ERR_STATE, "the RVE already belongs to a batch");
     if (r->precision != b->precision) return fail(VOCE_ERR_ARG, "precision differs from the batch's");
     int rc = ensure_ring(r, n_increments + 1);
