@@ -78,6 +78,15 @@ def test_reader_errors(voce_lib):
     with pytest.raises(capi.VoceError) as e:
         capi.read_mesh(os.path.join(d, "mesh.txt"), (4, 4, 4))
     assert e.value.code == 3
+    # an index far out of range (17 digits, whose linear index exceeds 64
+    # bits on a 1 x 10 x 10 grid) is an index mismatch, with no overflow in
+    # the index arithmetic (the sanitizer run checks that)
+    rows = ["0.0 0.0 0.0 1 %d %d 1 1" % (j + 1, k + 1) for j in range(10) for k in range(10)]
+    rows[7] = "0.0 0.0 0.0 99999999999999999 99999999999999999 -99999999999999999 1 1"
+    open(os.path.join(d, "mesh.txt"), "w").write("\n".join(rows) + "\n")
+    with pytest.raises(capi.VoceError) as e:
+        capi.read_mesh(os.path.join(d, "mesh.txt"), (1, 10, 10))
+    assert e.value.code == 3 and "index" in str(e.value) and "voxel 7" in str(e.value)
 
 
 def test_create_refuses_bad_inputs_before_the_gpu(voce_lib):

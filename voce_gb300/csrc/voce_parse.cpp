@@ -150,8 +150,11 @@ void parse_chunk(Chunk &c, const int dims[3], long long nv, double *eul, int *gr
             c.why = 1;
             return;
         }
-        const long long idx = ((iv[0] - 1) * (long long)dims[1] + iv[1] - 1) * dims[2] + iv[2] - 1;
-        if (idx != v) {
+        // modulo 2^64, so that no index of up to 17 digits overflows; an
+        // index whose exact linear value is v gives v
+        const uint64_t idx = ((uint64_t)(iv[0] - 1) * (uint64_t)dims[1] + (uint64_t)(iv[1] - 1)) *
+                                 (uint64_t)dims[2] + (uint64_t)(iv[2] - 1);
+        if (idx != (uint64_t)v) {
             c.bad = v;
             c.why = 2;
             return;
