@@ -89,6 +89,60 @@ def test_reader_errors(voce_lib):
     assert e.value.code == 3 and "index" in str(e.value) and "voxel 7" in str(e.value)
 
 
+def test_readers_on_edited_files(voce_lib):
+    """The namelist, .sx and mesh readers, and creation's host checks, on 300
+    randomly edited input files (characters replaced, inserted, deleted or
+    copied from elsewhere in the file; seeded): each call returns a result or
+    a status code.  Under the sanitizer run this is a small fuzz test of the
+    host parsers."""
+    import random
+    rng = random.Random(11)
+    case = synth.small_case(4, 2, 3, n_steps=1)
+    d, nlp = _case_dir(case)
+    names = {"nl": os.path.basename(nlp), "sx": "mat.sx", "mesh": "mesh.txt"}
+    text = {k: open(os.path.join(d, f)).read() for k, f in names.items()}
+    alphabet = "0123456789.-+eEnaifx \t\n,#"
+
+    def edit(t):
+        t = list(t)
+        for _ in range(rng.randint(1, 8)):
+            i, op = rng.randrange(max(1, len(t))), rng.random()
+            if op < 0.4 and t:
+                t[i] = rng.choice(alphabet)
+            elif op < 0.6:
+                t.insert(i, rng.choice(alphabet) * rng.randint(1, 120))
+            elif op < 0.8 and t:
+                del t[i:i + rng.randint(1, 40)]
+            else:
+                j = rng.randrange(max(1, len(t)))
+                t[i:i] = t[j:j + rng.randint(1, 60)]
+        return "".join(t)
+
+    try:
+        capi.device_memory()
+        host_only = False       # a GPU is present: creation would run on it; skip that part
+    except capi.VoceError:
+        host_only = True
+    outcomes = {"ok": 0, "refused": 0}
+    for _ in range(300):
+        which = rng.choice(sorted(names))
+        for k, f in names.items():
+            open(os.path.join(d, f), "w").write(edit(text[k]) if k == which else text[k])
+        try:
+            nl = capi.read_namelist(os.path.join(d, names["nl"]))
+            sx = capi.read_slip(os.path.join(d, names["sx"]))
+            dims = tuple(nl.CellDim)
+            if all(0 < x <= 64 for x in dims):
+                eul, gr, ph = capi.read_mesh(os.path.join(d, names["mesh"]), dims)
+                if host_only:
+                    with pytest.raises(capi.VoceError):     # refused on the host, or at the GPU
+                        capi.Rve.create(nl, sx, eul, gr, ph)
+            outcomes["ok"] += 1
+        except capi.VoceError:
+            outcomes["refused"] += 1
+    assert outcomes["ok"] > 50 and outcomes["refused"] > 50, outcomes
+
+
 def test_create_refuses_bad_inputs_before_the_gpu(voce_lib):
     """Host-side fault injection (no GPU touched): a NaN Euler angle in the
     mesh buffer, a singular crystal stiffness (C11 = C12, init.c:120-135 would
@@ -104,6 +158,15 @@ def test_create_refuses_bad_inputs_before_the_gpu(voce_lib):
     with pytest.raises(capi.VoceError) as e:
         capi.Rve.create(nl, sx, eul, case.mesh.grain, case.mesh.phase)
     assert e.value.code == 1 and "non-finite" in str(e.value)
+    # an x edge of 1152 points: an FP64 line does not fit a block's shared
+    # memory in the FFT passes (refused before the GPU; FP32 lines fit)
+    dims = (1152, 4, 4)
+    big = capi.read_namelist(nlp)
+    big.CellDim[0], big.CellDim[1], big.CellDim[2] = dims
+    nv = int(np.prod(dims))
+    with pytest.raises(capi.VoceError) as e:
+        capi.Rve.create(big, sx, np.zeros((nv, 3)), np.ones(nv, np.int32), np.ones(nv, np.int32))
+    assert e.value.code == 6 and "too long" in str(e.value), str(e.value)
     ph = case.mesh.phase.copy()
     ph[3] = 3
     with pytest.raises(capi.VoceError) as e:

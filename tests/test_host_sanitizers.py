@@ -2,7 +2,9 @@
 UndefinedBehaviorSanitizer (no GPU needed): a copy of libvoce_gpu.so built
 with both sanitizers in its host code runs the host-side tests of
 tests/test_capi_host.py -- the namelist, .sx and mesh readers on valid and
-malformed inputs (the chunked decimal parser included), the footprint, the
+malformed inputs (the chunked decimal parser included, and 300 randomly
+edited input files through the readers and creation's host checks), the
+footprint, the
 rejection of damaged snapshots and the server's queue, cancellation and
 deadline handling -- in a child process with the sanitizer runtimes
 preloaded.  Any invalid memory access or undefined behaviour stops that

@@ -447,6 +447,7 @@ namespace {
 int autotune_tiles(voce_rve *r);
 void apply_tiles(voce_rve *r, const Tiles &t);
 Tiles tiles_of(const RveDesc &d);
+FftPlan1 schedule_of(int L, bool mixed, int k);
 extern int g_autotune;
 extern int g_newton_chord;
 extern int g_ir_predictor;
@@ -730,6 +731,27 @@ int voce_rve_create(const voce_namelist *nl, const voce_slip *slip[2], const voc
         t6_to_b<double>(ud, sc.d6);
         double s6[6] = {S[0], S[4], S[8], S[5], S[2], S[1]};
         t6_to_b<double>(s6, sc.sc6);
+    }
+
+    // the default tiles must fit in a block's shared memory; they keep to a
+    // budget well inside it and fall back to one line per tile when a line
+    // is longer, so this refuses a grid exactly when one line does not fit
+    // (in FP64, an x edge above 1024 points)
+    {
+        Tiles t;
+        if (d.mixed) t.choose<float>(d);
+        else t.choose<double>(d);
+        RveDesc dt = d;
+        dt.zrows = t.zrows; dt.yxt = t.yxt; dt.xkc = t.xkc;
+        dt.xkc3 = t.xkc3; dt.zirows = t.zirows; dt.zirows3 = t.zirows3;
+        dt.plx = schedule_of(nx, d.mixed != 0, 0);
+        dt.ply = schedule_of(ny, d.mixed != 0, 0);
+        dt.plz = schedule_of(nz, d.mixed != 0, 0);
+        for (int ph = BP_ZF; ph < BP_COUNT; ++ph)
+            if (batch_smem(dt, ph) > 227 * 1024)
+                return fail(VOCE_ERR_UNSUPPORTED,
+                            "grid %dx%dx%d: a line is too long for the FFT passes' shared memory in this precision",
+                            nx, ny, nz);
     }
 
     // device memory
