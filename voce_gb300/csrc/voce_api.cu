@@ -68,11 +68,11 @@ namespace {
 
 // ---- Lebensohn-Tome basis (kinematics.c:346-364) on the host ------------
 double HB[6][3][3];
-bool hb_ready = false;
+std::once_flag hb_once;
 
-void hb_init()
+// filled once per process; RVEs may be created from several host threads
+void hb_fill()
 {
-    if (hb_ready) return;
     std::memset(HB, 0, sizeof(HB));
     HB[1][0][0] = -1. * RSQ6; HB[1][1][1] = -1. * RSQ6; HB[1][2][2] = 2. * RSQ6;
     HB[0][0][0] = -1. * RSQ2; HB[0][1][1] = RSQ2;
@@ -80,8 +80,9 @@ void hb_init()
     HB[3][0][2] = RSQ2; HB[3][2][0] = RSQ2;
     HB[4][0][1] = RSQ2; HB[4][1][0] = RSQ2;
     HB[5][0][0] = RSQ3; HB[5][1][1] = RSQ3; HB[5][2][2] = RSQ3;
-    hb_ready = true;
 }
+
+void hb_init() { std::call_once(hb_once, hb_fill); }
 
 // chg_basis opt 2 (3x3 -> nb-vector) and opt 4 (3x3x3x3 -> 6x6), opt 3
 void t_to_v(const double t[3][3], double *v, int nb)

@@ -11,6 +11,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 
 namespace voce {
 
@@ -2574,9 +2575,10 @@ static const int kNrStageBytes = VOCE_STAGE_FLOATS * VOCE_NR_THREADS * (int)size
 // RVE is created, before any launch or stream capture.
 int nr_resident_blocks(int kind)
 {
-    static int cached[3] = {0, 0, 0};
-    int &c = cached[(kind >= 0 && kind < 3) ? kind : 0];
-    if (!c) {
+    // several host threads may ask at once: each computes the same value
+    static std::atomic<int> cached[3];
+    std::atomic<int> &c = cached[(kind >= 0 && kind < 3) ? kind : 0];
+    if (!c.load()) {
         int dev = 0, sms = 152, per = 2;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -2591,9 +2593,9 @@ int nr_resident_blocks(int kind)
         } else {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_nr<false>, VOCE_NR_THREADS, 0);
         }
-        c = sms * (per > 0 ? per : 1);
+        c.store(sms * (per > 0 ? per : 1));
     }
-    return c;
+    return c.load();
 }
 
 static int grid_for(int total, int cap)
