@@ -158,6 +158,16 @@ def test_create_refuses_bad_inputs_before_the_gpu(voce_lib):
     with pytest.raises(capi.VoceError) as e:
         capi.Rve.create(nl, sx, eul, case.mesh.grain, case.mesh.phase)
     assert e.value.code == 1 and "non-finite" in str(e.value)
+    # mesh arrays shorter than the grid never reach the library, which reads
+    # them through plain pointers
+    with pytest.raises(ValueError):
+        capi.Rve.create(nl, sx, case.mesh.euler_deg[:-1], case.mesh.grain, case.mesh.phase)
+    with pytest.raises(ValueError):
+        capi.Rve.create(nl, sx, case.mesh.euler_deg, case.mesh.grain[:5], case.mesh.phase)
+    with capi.Server(capi.PREC_FP64, 1 << 30) as srv, pytest.raises(ValueError):
+        srv.submit(nl, sx, case.mesh.euler_deg, case.mesh.grain, case.mesh.phase[1:], 1)
+    with pytest.raises(ValueError):
+        capi.mesh_voronoi((4, 4, 4), np.zeros((3, 3)), np.zeros((2, 3)))
     # an x edge of 1152 points: an FP64 line does not fit a block's shared
     # memory in the FFT passes (refused before the GPU; FP32 lines fit)
     dims = (1152, 4, 4)

@@ -217,6 +217,34 @@ def _iptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+def _mesh_arrays(dims: Sequence[int], euler_deg, grain, phase):
+    """The mesh arrays as the C ABI reads them (contiguous float64 Euler
+    angles of shape (nv, 3), int32 grain and phase ids of nv each), checked
+    against the grid: the library reads 3 nv + 2 nv values through plain
+    pointers and cannot check their lengths itself."""
+    nv = int(np.prod(dims))
+    eul = np.ascontiguousarray(euler_deg, dtype=np.float64)
+    gr = np.ascontiguousarray(grain, dtype=np.int32)
+    ph = np.ascontiguousarray(phase, dtype=np.int32)
+    if eul.size != 3 * nv or gr.size != nv or ph.size != nv:
+        raise ValueError("mesh arrays of %d Euler angles, %d grain ids and %d phase ids for a "
+                         "%s grid (%d voxels)" % (eul.size, gr.size, ph.size, tuple(dims), nv))
+    mesh = VoceMesh()
+    mesh.dims = (C.c_int * 3)(*dims)
+    mesh.euler_deg = _dptr(eul)
+    mesh.grain = _iptr(gr)
+    mesh.phase = _iptr(ph)
+    return mesh, (eul, gr, ph)
+
+
+def _slip_pair(slip: "VoceSlip", solid_phase: int):
+    if solid_phase not in (0, 1):
+        raise ValueError("solid_phase %r: 0 or 1" % (solid_phase,))
+    sp = (C.POINTER(VoceSlip) * 2)()
+    sp[solid_phase] = C.pointer(slip)
+    return sp
+
+
 def read_namelist(path: str) -> VoceNamelist:
     nl = VoceNamelist()
     _check(load().voce_namelist_read(path.encode(), C.byref(nl)))
@@ -233,8 +261,10 @@ def mesh_voronoi(dims: Sequence[int], seeds: np.ndarray, grain_euler_deg: np.nda
     """voce_mesh_voronoi: (euler (nv, 3), grain, phase) of the periodic Voronoi
     tessellation of the grid by `seeds` (n, 3), computed on the GPU."""
     nv = int(np.prod(dims))
-    s = np.ascontiguousarray(seeds, dtype=np.float64)
+    s = np.ascontiguousarray(seeds, dtype=np.float64).reshape(-1, 3)
     ge = np.ascontiguousarray(grain_euler_deg, dtype=np.float64)
+    if ge.size != s.size:
+        raise ValueError("%d seeds and %d grain orientations" % (len(s), ge.size // 3))
     eul = np.zeros((nv, 3))
     grain = np.zeros(nv, dtype=np.int32)
     phase = np.zeros(nv, dtype=np.int32)
@@ -310,16 +340,8 @@ class Rve:
                grain: np.ndarray, phase: np.ndarray, precision: int = PREC_FP64,
                solid_phase: int = 0) -> "Rve":
         lib = load()
-        eul = np.ascontiguousarray(euler_deg, dtype=np.float64)
-        gr = np.ascontiguousarray(grain, dtype=np.int32)
-        ph = np.ascontiguousarray(phase, dtype=np.int32)
-        mesh = VoceMesh()
-        mesh.dims = (C.c_int * 3)(*nl.CellDim)
-        mesh.euler_deg = _dptr(eul)
-        mesh.grain = _iptr(gr)
-        mesh.phase = _iptr(ph)
-        sp = (C.POINTER(VoceSlip) * 2)()
-        sp[solid_phase] = C.pointer(slip)
+        mesh, keep = _mesh_arrays(tuple(nl.CellDim), euler_deg, grain, phase)
+        sp = _slip_pair(slip, solid_phase)
         h = C.c_void_p()
         _check(lib.voce_rve_create(C.byref(nl), sp, C.byref(mesh), precision, C.byref(h)))
         return cls(h, tuple(nl.CellDim))
@@ -615,16 +637,8 @@ class Server:
 
     def submit(self, nl: VoceNamelist, slip: VoceSlip, euler_deg, grain, phase,
                n_increments: int, solid_phase: int = 0) -> int:
-        eul = np.ascontiguousarray(euler_deg, dtype=np.float64)
-        gr = np.ascontiguousarray(grain, dtype=np.int32)
-        ph = np.ascontiguousarray(phase, dtype=np.int32)
-        mesh = VoceMesh()
-        mesh.dims = (C.c_int * 3)(*nl.CellDim)
-        mesh.euler_deg = _dptr(eul)
-        mesh.grain = _iptr(gr)
-        mesh.phase = _iptr(ph)
-        sp = (C.POINTER(VoceSlip) * 2)()
-        sp[solid_phase] = C.pointer(slip)
+        mesh, keep = _mesh_arrays(tuple(nl.CellDim), euler_deg, grain, phase)
+        sp = _slip_pair(slip, solid_phase)
         rid = C.c_longlong()
         _check(load().voce_server_submit(self._h, C.byref(nl), sp, C.byref(mesh), n_increments,
                                          C.byref(rid)))
