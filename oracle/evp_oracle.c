@@ -300,7 +300,7 @@ static int update_stress_voxel(int nsys, const double *cgr, const double *c066,
 {
     double sg66[6][6], aux[3][3], strain_aux[3][3];
     double xl6[6], sig6[6], eps6[6], strain6[6], edot6[6], d66[6][6];
-    double tot_eps[6], sig6_old[6], res[6], jac[6][6];
+    double tot_eps[6] = {0}, sig6_old[6], res[6], jac[6][6];   /* set by the first Newton pass, which always runs */
     memcpy(sg66, cgr, sizeof(sg66));
     int rc = lu_inv6(sg66);
     if (rc) return rc;
